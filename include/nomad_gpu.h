@@ -1,0 +1,184 @@
+/*
+ * nomad_gpu.h -- C-ABI of the GB300 NOMAD matrix-completion library.
+ *
+ * Single-GPU, sm_103a.  The library owns all device memory of a context; every
+ * argument is a plain pointer or scalar.  No C++ types and no exceptions cross
+ * this boundary; every call returns a status (0 = OK, < 0 = error).
+ *
+ * Reference entry points each call replaces (yxtj/nomad, paths inside the project):
+ *   nomad_gpu_init         NomadBody::initial (Code/nomad/nb_init.cpp:189-235), the
+ *                          per-worker CSC build of read_data (nb_data.cpp:131-169),
+ *                          row init (nb_main.cpp:443-456) and column-token init
+ *                          (nb_main.cpp:67-98)
+ *   nomad_gpu_epoch        one training interval of NomadBody::run
+ *                          (nb_main.cpp:109-135) running NomadBody::updater_func's
+ *                          training loop (nb_main.cpp:480-572) on every worker
+ *   nomad_gpu_sse /        the evaluation pass (nb_main.cpp:577-676) and the
+ *   nomad_gpu_rmse         statistics block (nb_main.cpp:215-285)
+ *   nomad_gpu_get_factors  the --output dump of rows and columns
+ *                          (nb_main.cpp:349-366, 683-705)
+ *   nomad_gpu_destroy      teardown (nb_main.cpp:368-408)
+ */
+#ifndef NOMAD_GPU_H_
+#define NOMAD_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NOMAD_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------------- */
+enum nomad_gpu_status {
+  NOMAD_OK = 0,
+  NOMAD_ERR_INVALID_ARG = -1, /* bad sizes, indices out of range, null pointers   */
+  NOMAD_ERR_CUDA = -2,        /* a CUDA runtime call failed                       */
+  NOMAD_ERR_OOM = -3,         /* device or host allocation failed                 */
+  NOMAD_ERR_TIMEOUT = -4,     /* a bounded device wait ran out (no global progress) */
+  NOMAD_ERR_BOUNDS = -5,      /* a device-side bounds check failed                */
+  NOMAD_ERR_IO = -6,          /* file could not be opened / read / written        */
+  NOMAD_ERR_FORMAT = -7,      /* file is not a train.dat/test.dat binary matrix   */
+  NOMAD_ERR_NO_DEVICE = -8,   /* no CUDA device, or not an sm_103 device          */
+  NOMAD_ERR_UNSUPPORTED = -9  /* combination of options not supported             */
+};
+
+/* ---- options ------------------------------------------------------------------ */
+enum nomad_gpu_mode {
+  NOMAD_MODE_ASYNC = 0,  /* NOMAD: worker warps pass column tokens through queues */
+  NOMAD_MODE_DSGD = 1,   /* DSGD stratum sweep (Code/competitor/sgd-mpi-omp.cpp)  */
+  NOMAD_MODE_REPLAY = 2  /* one worker, columns round-robin: deterministic order  */
+};
+enum nomad_gpu_precision {
+  NOMAD_PREC_FP32 = 0,   /* W, H stored in fp32                                   */
+  NOMAD_PREC_BF16_SR = 1 /* W, H stored in bf16, fp32 arithmetic, stochastic-
+                            rounding write-back                                   */
+};
+enum nomad_gpu_init_kind {
+  NOMAD_INIT_REFERENCE = 0, /* the reference's mt19937_64 streams (bit-identical) */
+  NOMAD_INIT_HASH = 1       /* U(0, 1/sqrt(dim)) from a counter hash, on device   */
+};
+
+typedef struct nomad_gpu_params {
+  int32_t struct_size; /* = sizeof(nomad_gpu_params); set by nomad_gpu_params_default */
+  int32_t dim;         /* --dim (latent dimension k)                   default 100   */
+  double lrate;        /* --lrate                                      default 0.001 */
+  double drate;        /* --drate                                      default 0.1   */
+  double reg;          /* --reg (lambda)                               default 1.0   */
+  uint64_t seed;       /* --seed                                       default 12345 */
+  int32_t mode;        /* nomad_gpu_mode                               default ASYNC */
+  int32_t precision;   /* nomad_gpu_precision                          default FP32  */
+  int32_t init;        /* nomad_gpu_init_kind (ignored when W0/H0 given) REFERENCE   */
+  int32_t init_parts;  /* row blocks of the reference init = ranks x --nthreads (1)  */
+  int32_t device;      /* CUDA device ordinal                          default 0     */
+  int32_t workers;     /* ASYNC: worker warps, 0 = every resident warp slot          */
+  int32_t warps_per_block; /* 0 = auto                                               */
+  int32_t blocks_per_sm;   /* 0 = as many as fit                                     */
+  int32_t balance;     /* row blocks: 0 = equal rows (reference), 1 = equal ratings  */
+  int32_t dsgd_inner_blocks; /* DSGD innerB (blocks per side), 0 = auto              */
+  int32_t dsgd_strategy;     /* DSGD stratum strategy: 0 semi-WOR, 2 WOR             */
+  int32_t exact;       /* 1: reference operation order (sequential dot, no FMA);
+                          REPLAY always uses it                                      */
+  int32_t spin_budget_ms; /* device waits give up after this long without global
+                             progress and the call returns NOMAD_ERR_TIMEOUT (2000)  */
+  int32_t debug_flags; /* test hooks; bit 0 = enqueue no tokens (forces a timeout)   */
+  int32_t reserved[8];
+} nomad_gpu_params;
+
+/* One rating set in either the reference's row-major file layout (row_counts !=
+ * NULL: entries listed row by row, as train.dat stores them, nb_data.cpp:40-64) or
+ * COO (rows != NULL).  Exactly one of vals_f64 / vals_f32 is non-NULL. */
+typedef struct nomad_gpu_matrix {
+  int64_t nnz;
+  const int32_t* row_counts; /* [m]   or NULL                                      */
+  const int32_t* rows;       /* [nnz] or NULL                                      */
+  const int32_t* cols;       /* [nnz]                                              */
+  const double* vals_f64;    /* [nnz] or NULL                                      */
+  const float* vals_f32;     /* [nnz] or NULL                                      */
+} nomad_gpu_matrix;
+
+typedef struct nomad_gpu_problem {
+  int32_t m;              /* rows (users)                                          */
+  int32_t n;              /* columns (items): one token each                      */
+  nomad_gpu_matrix train;
+  nomad_gpu_matrix test;  /* nnz may be 0                                          */
+  const float* W0;        /* optional initial rows    [m * dim], row-major         */
+  const float* H0;        /* optional initial columns [n * dim], row-major         */
+} nomad_gpu_problem;
+
+typedef struct nomad_gpu_epoch_stats {
+  int64_t updates;     /* ratings visited (the reference's u=)                     */
+  int64_t hops;        /* token hand-offs between workers                          */
+  int64_t failures;    /* empty queue polls (the reference's f=)                   */
+  int32_t epochs_done; /* cumulative epochs after this call                        */
+  int32_t reserved0;
+  double device_ms;    /* CUDA-event time of the call's device work on its stream  */
+  double host_seconds; /* wall time of the call                                    */
+  double online_sse;   /* sum of e^2 seen while training (ColumnData::error)       */
+} nomad_gpu_epoch_stats;
+
+typedef struct nomad_gpu_info {
+  int32_t m, n, dim, dim_padded;
+  int64_t nnz_train, nnz_test;
+  int32_t workers;          /* ASYNC worker warps (REPLAY: 1)                      */
+  int32_t active_tokens;    /* columns with at least one training rating          */
+  int64_t segments;         /* non-empty (worker, column) visits per epoch         */
+  int64_t max_column;       /* largest column (ratings)                            */
+  int32_t grid_blocks, block_threads, num_sms, inner_blocks;
+  int64_t device_bytes;     /* device memory held by the context                   */
+  int32_t mode, precision;
+} nomad_gpu_info;
+
+typedef struct nomad_gpu_ctx nomad_gpu_ctx; /* opaque */
+
+/* ---- API ------------------------------------------------------------------------ */
+
+/* Fill *p with the reference's defaults (nomad_option.cpp:16-77). */
+int nomad_gpu_params_default(nomad_gpu_params* p);
+
+/* Copy the problem to the device, build the layout and initialise W and H.  Host
+ * buffers stay owned by the caller and are not referenced after the call. */
+int nomad_gpu_init(nomad_gpu_ctx** out, const nomad_gpu_problem* prob,
+                   const nomad_gpu_params* params);
+
+/* Run n_epochs epochs.  One epoch = every training rating is visited once: in ASYNC
+ * every column token makes one full pass over the workers that hold its ratings; the
+ * step size of a visit uses the token's pass count (nb_main.cpp:514-515).  Blocks
+ * until the device work is done; st may be NULL. */
+int nomad_gpu_epoch(nomad_gpu_ctx* ctx, int32_t n_epochs, nomad_gpu_epoch_stats* st);
+
+/* Squared-error sums and counts over the training and test sets (nb_main.cpp:617-653);
+ * FP64 accumulation on the device. Any pointer may be NULL. */
+int nomad_gpu_sse(nomad_gpu_ctx* ctx, double* train_sse, int64_t* train_count,
+                  double* test_sse, int64_t* test_count);
+
+/* RMSE = sqrt(sse / count) for both sets (nb_main.cpp:272-275). */
+int nomad_gpu_rmse(nomad_gpu_ctx* ctx, double* train_rmse, double* test_rmse);
+
+/* Copy the factors to host float arrays W[m*dim], H[n*dim] (either may be NULL). */
+int nomad_gpu_get_factors(nomad_gpu_ctx* ctx, float* W, float* H);
+
+/* Overwrite the factors from host float arrays (either may be NULL). */
+int nomad_gpu_set_factors(nomad_gpu_ctx* ctx, const float* W, const float* H);
+
+/* Describe the context (sizes, workers, segments, memory). */
+int nomad_gpu_get_info(nomad_gpu_ctx* ctx, nomad_gpu_info* info);
+
+/* Free every device and host resource of the context.  NULL is a no-op. */
+void nomad_gpu_destroy(nomad_gpu_ctx* ctx);
+
+/* Static description of a status code. */
+const char* nomad_gpu_strerror(int status);
+
+/* Detail of the most recent failing call made by this thread ("" if none). */
+const char* nomad_gpu_last_error(void);
+
+/* 1 when a usable sm_103 device is present, else 0. */
+int nomad_gpu_device_ok(int32_t device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NOMAD_GPU_H_ */

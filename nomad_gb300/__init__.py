@@ -1,0 +1,231 @@
+"""nomad_gb300 -- NOMAD asynchronous SGD matrix completion on one GB300 (sm_103a).
+
+Python face of libnomad_gpu.so.  The library's C-ABI (include/nomad_gpu.h,
+include/nomad_io.h) is the product; this module wraps it with numpy arrays:
+
+    train, test = nomad_gb300.synth(1)                 # or RatingMatrix.read(path)
+    with nomad_gb300.Nomad(train, test, dim=100, lrate=0.001, drate=0.1, reg=0.05) as nm:
+        stats = nm.epoch(1)
+        train_rmse, test_rmse = nm.rmse()
+
+Every call goes to the CUDA library; there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import NomadError, check, lib  # noqa: F401
+
+MODES = {"async": _abi.MODE_ASYNC, "dsgd": _abi.MODE_DSGD, "replay": _abi.MODE_REPLAY}
+PRECISIONS = {"fp32": _abi.PREC_FP32, "bf16": _abi.PREC_BF16_SR}
+INITS = {"reference": _abi.INIT_REFERENCE, "hash": _abi.INIT_HASH}
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class _Owned:
+    """Keeps library-owned arrays of an nomad_io_matrix alive; frees them on collection."""
+
+    def __init__(self, io):
+        self.io = io
+
+    def __del__(self):
+        try:
+            lib().nomad_io_free(ctypes.byref(self.io))
+        except Exception:  # interpreter shutdown
+            pass
+
+
+def _wrap(ptr, count, ctype, dtype, owner):
+    if count == 0:
+        return np.zeros(0, dtype)
+    arr_t = ctype * count
+    buf = arr_t.from_address(ctypes.addressof(ptr.contents))
+    buf._owner = owner
+    return np.frombuffer(buf, dtype=dtype)
+
+
+class RatingMatrix:
+    """A rating set in the train.dat row-major layout: row_counts[m], cols[nnz], vals[nnz]."""
+
+    def __init__(self, m, n, row_counts, cols, vals, file_id=0):
+        self.m, self.n = int(m), int(n)
+        self.row_counts = np.ascontiguousarray(row_counts, np.int32)
+        self.cols = np.ascontiguousarray(cols, np.int32)
+        self.vals = np.ascontiguousarray(vals, np.float64)
+        self.file_id = int(file_id)
+        assert self.row_counts.shape == (self.m,)
+        assert self.cols.shape == self.vals.shape
+
+    @property
+    def nnz(self):
+        return int(self.cols.size)
+
+    @classmethod
+    def _from_io(cls, io):
+        owner = _Owned(io)
+        return cls(io.m, io.n,
+                   _wrap(io.row_counts, io.m, ctypes.c_int32, np.int32, owner),
+                   _wrap(io.cols, io.nnz, ctypes.c_int32, np.int32, owner),
+                   _wrap(io.vals, io.nnz, ctypes.c_double, np.float64, owner), io.file_id)
+
+    @classmethod
+    def read(cls, path):
+        io = _abi.IoMatrix()
+        check(lib().nomad_io_read(os.fsencode(path), ctypes.byref(io)), "nomad_io_read")
+        return cls._from_io(io)
+
+    def write(self, path, file_id=0):
+        check(lib().nomad_io_write(os.fsencode(path), self.m, self.n, self.nnz,
+                                   _ptr(self.row_counts), _ptr(self.cols), _ptr(self.vals),
+                                   file_id), "nomad_io_write")
+
+    def rows(self):
+        """Row index of every entry (COO rows)."""
+        return np.repeat(np.arange(self.m, dtype=np.int32), self.row_counts)
+
+    def to_csc(self):
+        """(col_ptr int64[n+1], row_idx int32[nnz], vals float64[nnz]), rows ascending."""
+        rows = self.rows()
+        order = np.lexsort((rows, self.cols))
+        col_ptr = np.zeros(self.n + 1, np.int64)
+        np.cumsum(np.bincount(self.cols, minlength=self.n), out=col_ptr[1:])
+        return col_ptr, rows[order].astype(np.int32), self.vals[order]
+
+    def _c(self):
+        return _abi.Matrix(self.nnz, _ptr(self.row_counts), None, _ptr(self.cols),
+                           _ptr(self.vals), None)
+
+
+def read_header(path):
+    fid, m, n, nnz = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+    check(lib().nomad_io_read_header(os.fsencode(path), ctypes.byref(fid), ctypes.byref(m),
+                                     ctypes.byref(n), ctypes.byref(nnz)), "nomad_io_read_header")
+    return {"file_id": fid.value, "m": m.value, "n": n.value, "nnz": nnz.value}
+
+
+def synth_spec(workload, **overrides):
+    spec = _abi.SynthSpec()
+    check(lib().nomad_synth_preset(int(workload), ctypes.byref(spec)), "nomad_synth_preset")
+    for k, v in overrides.items():
+        setattr(spec, k, v)
+    return spec
+
+
+def synth(workload_or_spec, **overrides):
+    """Generate (train, test) RatingMatrix for a named workload (1-4) or a SynthSpec."""
+    spec = workload_or_spec if isinstance(workload_or_spec, _abi.SynthSpec) else \
+        synth_spec(workload_or_spec, **overrides)
+    tr, te = _abi.IoMatrix(), _abi.IoMatrix()
+    check(lib().nomad_synth_generate(ctypes.byref(spec), ctypes.byref(tr), ctypes.byref(te)),
+          "nomad_synth_generate")
+    return RatingMatrix._from_io(tr), RatingMatrix._from_io(te)
+
+
+def reference_init(m, n, dim, seed=12345, parts=1):
+    """The reference's initial factors (float32 W[m,dim], H[n,dim])."""
+    W = np.empty((m, dim), np.float32)
+    H = np.empty((n, dim), np.float32)
+    check(lib().nomad_reference_init(m, n, dim, seed, parts, _ptr(W), _ptr(H)),
+          "nomad_reference_init")
+    return W, H
+
+
+def write_factors(path, W, H):
+    W = np.ascontiguousarray(W, np.float32)
+    H = np.ascontiguousarray(H, np.float32)
+    check(lib().nomad_io_write_factors(os.fsencode(path), W.shape[0], H.shape[0], W.shape[1],
+                                       _ptr(W), _ptr(H)), "nomad_io_write_factors")
+
+
+def default_params(**overrides):
+    p = _abi.Params()
+    check(lib().nomad_gpu_params_default(ctypes.byref(p)), "nomad_gpu_params_default")
+    for k, v in overrides.items():
+        if k == "mode":
+            v = MODES[v] if isinstance(v, str) else v
+        elif k == "precision":
+            v = PRECISIONS[v] if isinstance(v, str) else v
+        elif k == "init":
+            v = INITS[v] if isinstance(v, str) else v
+        setattr(p, k, v)
+    return p
+
+
+def device_ok(device=0):
+    return bool(lib().nomad_gpu_device_ok(device))
+
+
+class Nomad:
+    """One training context on the GPU (nomad_gpu_ctx)."""
+
+    def __init__(self, train, test=None, W0=None, H0=None, params=None, **kw):
+        self._ctx = ctypes.c_void_p()
+        p = params if params is not None else default_params(**kw)
+        self.params = p
+        if test is None:
+            test = RatingMatrix(train.m, train.n, np.zeros(train.m, np.int32),
+                                np.zeros(0, np.int32), np.zeros(0))
+        self.m, self.n, self.dim = train.m, train.n, p.dim
+        W0 = None if W0 is None else np.ascontiguousarray(W0, np.float32)
+        H0 = None if H0 is None else np.ascontiguousarray(H0, np.float32)
+        if W0 is not None:
+            assert W0.shape == (self.m, self.dim)
+        if H0 is not None:
+            assert H0.shape == (self.n, self.dim)
+        prob = _abi.Problem(train.m, train.n, train._c(), test._c(), _ptr(W0), _ptr(H0))
+        check(lib().nomad_gpu_init(ctypes.byref(self._ctx), ctypes.byref(prob), ctypes.byref(p)),
+              "nomad_gpu_init")
+
+    def epoch(self, n_epochs=1):
+        st = _abi.EpochStats()
+        check(lib().nomad_gpu_epoch(self._ctx, n_epochs, ctypes.byref(st)), "nomad_gpu_epoch")
+        return {k: getattr(st, k) for k, _ in _abi.EpochStats._fields_ if k != "reserved0"}
+
+    def sse(self):
+        a, c, b, d = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+        check(lib().nomad_gpu_sse(self._ctx, ctypes.byref(a), ctypes.byref(c), ctypes.byref(b),
+                                  ctypes.byref(d)), "nomad_gpu_sse")
+        return a.value, c.value, b.value, d.value
+
+    def rmse(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(lib().nomad_gpu_rmse(self._ctx, ctypes.byref(a), ctypes.byref(b)), "nomad_gpu_rmse")
+        return a.value, b.value
+
+    def factors(self):
+        W = np.empty((self.m, self.dim), np.float32)
+        H = np.empty((self.n, self.dim), np.float32)
+        check(lib().nomad_gpu_get_factors(self._ctx, _ptr(W), _ptr(H)), "nomad_gpu_get_factors")
+        return W, H
+
+    def set_factors(self, W=None, H=None):
+        W = None if W is None else np.ascontiguousarray(W, np.float32)
+        H = None if H is None else np.ascontiguousarray(H, np.float32)
+        check(lib().nomad_gpu_set_factors(self._ctx, _ptr(W), _ptr(H)), "nomad_gpu_set_factors")
+
+    def info(self):
+        i = _abi.Info()
+        check(lib().nomad_gpu_get_info(self._ctx, ctypes.byref(i)), "nomad_gpu_get_info")
+        return {k: getattr(i, k) for k, _ in _abi.Info._fields_}
+
+    def close(self):
+        if self._ctx:
+            lib().nomad_gpu_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

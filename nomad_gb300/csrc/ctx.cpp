@@ -1,0 +1,618 @@
+// ctx.cpp -- the C-ABI of libnomad_gpu (include/nomad_gpu.h): context lifetime, device
+// memory, layout upload and the launch sequence of each call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "common.h"
+#include "launch.h"
+#include "layout.h"
+
+using nomad::DevFactors;
+
+struct nomad_gpu_ctx {
+  nomad_gpu_params prm{};
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DevFactors f;
+  std::vector<void*> allocs;
+  int64_t device_bytes = 0;
+  // rating sets (CSC by column)
+  int2* train = nullptr;
+  int64_t* train_ptr = nullptr;
+  int64_t nnz_train = 0;
+  int2* test = nullptr;
+  int64_t* test_ptr = nullptr;
+  int64_t nnz_test = 0;
+  int64_t max_column = 0;
+  // async NOMAD
+  int4* segs = nullptr;
+  int64_t* vl_ptr = nullptr;
+  int32_t *tok_pos = nullptr, *tok_epoch = nullptr;
+  int32_t *qnext = nullptr, *qtail = nullptr, *qnext0 = nullptr, *qtail0 = nullptr;
+  int32_t* ctrl = nullptr;
+  unsigned long long *progress = nullptr, *stats = nullptr;
+  double* err_sum = nullptr;
+  int32_t P = 0, n_active = 0, grid = 0, wpb = 0;
+  int64_t n_segments = 0;
+  // DSGD
+  int4* rates = nullptr;
+  int64_t* blk_ptr = nullptr;
+  int32_t* sched = nullptr;
+  int32_t innerB = 0;
+  // step sizes per pass count
+  float* steps = nullptr;
+  int32_t n_steps = 0;
+  // evaluation scratch
+  double* partials = nullptr;
+  double* sse_out = nullptr;
+  int32_t sse_grid = 0;
+  int32_t epochs_done = 0;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+  nomad::set_last_error("%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? NOMAD_ERR_OOM : NOMAD_ERR_CUDA;
+}
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+template <typename T>
+int dalloc(nomad_gpu_ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    nomad::set_last_error("cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    cudaGetLastError();
+    return NOMAD_ERR_OOM;
+  }
+  c->allocs.push_back(q);
+  c->device_bytes += static_cast<int64_t>(bytes);
+  *p = static_cast<T*>(q);
+  return NOMAD_OK;
+}
+
+template <typename T>
+int upload(nomad_gpu_ctx* c, T** p, const T* src, size_t count) {
+  int rc = dalloc(c, p, count);
+  if (rc) return rc;
+  if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  return NOMAD_OK;
+}
+
+#define RC(call)               \
+  do {                         \
+    int rc_ = (call);          \
+    if (rc_) return rc_;       \
+  } while (0)
+
+int ensure_steps(nomad_gpu_ctx* c, int32_t needed) {
+  if (needed <= c->n_steps) return NOMAD_OK;
+  int32_t cap = std::max<int32_t>(64, c->n_steps);
+  while (cap < needed) cap *= 2;
+  std::vector<float> h(cap);
+  for (int32_t e = 0; e < cap; ++e) h[e] = nomad::step_size_f32(c->prm.lrate, c->prm.drate, e);
+  float* d = nullptr;
+  RC(dalloc(c, &d, cap));
+  CK(cudaMemcpyAsync(d, h.data(), cap * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->steps = d;  // the previous table stays allocated until destroy (small)
+  c->n_steps = cap;
+  return NOMAD_OK;
+}
+
+// Upload a dense fp32 [rows x dim] host array into padded storage, in chunks through
+// a bounded staging buffer.
+int put_factor(nomad_gpu_ctx* c, void* dst, const float* src, int64_t rows) {
+  const DevFactors& f = c->f;
+  const int64_t chunk_rows = std::max<int64_t>(1, (int64_t(16) << 20) / std::max(f.dim, 1));
+  float* stage = nullptr;
+  CK(cudaMalloc(&stage, std::max<int64_t>(1, std::min(rows, chunk_rows)) * f.dim * sizeof(float)));
+  const size_t esz = f.bf16 ? 2 : 4;
+  int rc = NOMAD_OK;
+  for (int64_t r0 = 0; r0 < rows && rc == NOMAD_OK; r0 += chunk_rows) {
+    const int64_t nr = std::min(chunk_rows, rows - r0);
+    cudaError_t e = cudaMemcpyAsync(stage, src + r0 * f.dim, nr * f.dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = nomad::launch_f32_to_store(stage, static_cast<char*>(dst) + r0 * f.kpad * esz, nr, f.dim,
+                                     f.kpad, f.bf16, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "factor upload");
+  }
+  cudaFree(stage);
+  return rc;
+}
+
+int get_factor(nomad_gpu_ctx* c, const void* src, float* dst, int64_t rows) {
+  const DevFactors& f = c->f;
+  const int64_t chunk_rows = std::max<int64_t>(1, (int64_t(16) << 20) / std::max(f.dim, 1));
+  float* stage = nullptr;
+  CK(cudaMalloc(&stage, std::max<int64_t>(1, std::min(rows, chunk_rows)) * f.dim * sizeof(float)));
+  const size_t esz = f.bf16 ? 2 : 4;
+  int rc = NOMAD_OK;
+  for (int64_t r0 = 0; r0 < rows && rc == NOMAD_OK; r0 += chunk_rows) {
+    const int64_t nr = std::min(chunk_rows, rows - r0);
+    cudaError_t e = nomad::launch_store_to_f32(static_cast<const char*>(src) + r0 * f.kpad * esz,
+                                               stage, nr, f.dim, f.kpad, f.bf16, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dst + r0 * f.dim, stage, nr * f.dim * sizeof(float),
+                          cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "factor download");
+  }
+  cudaFree(stage);
+  return rc;
+}
+
+int upload_csc(nomad_gpu_ctx* c, const nomad::Csc& csc, int2** ratings, int64_t** ptr) {
+  RC(upload(c, ptr, csc.col_ptr.data(), csc.col_ptr.size()));
+  RC(upload(c, ratings, reinterpret_cast<const int2*>(csc.ratings.data()), csc.ratings.size()));
+  return NOMAD_OK;
+}
+
+int reset_tokens(nomad_gpu_ctx* c) {
+  const int32_t n = c->f.n;
+  std::vector<int32_t> ep(static_cast<size_t>(std::max(n, 1)), c->epochs_done);
+  CK(cudaMemsetAsync(c->tok_pos, 0, sizeof(int32_t) * std::max(n, 1), c->stream));
+  CK(cudaMemcpyAsync(c->tok_epoch, ep.data(), sizeof(int32_t) * std::max(n, 1),
+                     cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return NOMAD_OK;
+}
+
+int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
+  const nomad_gpu_params& p = c->prm;
+  const int threads = nomad::host_threads();
+  CK(cudaSetDevice(c->device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, c->device));
+  if (prop.major * 10 + prop.minor != 103)
+    NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", c->device,
+               prop.major, prop.minor);
+  if (!prop.cooperativeLaunch) NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device lacks cooperative launch");
+  c->num_sms = prop.multiProcessorCount;
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&c->ev0));
+  CK(cudaEventCreate(&c->ev1));
+
+  // ---- factors -----------------------------------------------------------------
+  DevFactors& f = c->f;
+  f.m = prob->m;
+  f.n = prob->n;
+  f.dim = p.dim;
+  f.bf16 = p.precision == NOMAD_PREC_BF16_SR;
+  const int E = f.bf16 ? 8 : 4;
+  f.kpad = (p.dim + E - 1) / E * E;
+  f.nvec = f.kpad / E;
+  if (f.nvec > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "dim %d exceeds the supported maximum", p.dim);
+  f.red_width = 1;
+  while (f.red_width < std::min(f.nvec, 32)) f.red_width <<= 1;
+  const size_t esz = f.bf16 ? 2 : 4;
+  char* Wd = nullptr;
+  char* Hd = nullptr;
+  RC(dalloc(c, &Wd, static_cast<size_t>(f.m) * f.kpad * esz));
+  RC(dalloc(c, &Hd, static_cast<size_t>(f.n) * f.kpad * esz));
+  f.W = Wd;
+  f.H = Hd;
+  if (p.init == NOMAD_INIT_HASH && !(prob->W0 && prob->H0)) {
+    CK(nomad::launch_init_hash(f, p.seed, c->stream));
+  }
+  if (prob->W0) {
+    RC(put_factor(c, f.W, prob->W0, f.m));
+  } else if (p.init != NOMAD_INIT_HASH) {
+    std::vector<float> Wh(static_cast<size_t>(f.m) * f.dim);
+    RC(nomad_reference_init(f.m, 0, f.dim, p.seed, p.init_parts, Wh.data(), nullptr));
+    RC(put_factor(c, f.W, Wh.data(), f.m));
+  }
+  if (prob->H0) {
+    RC(put_factor(c, f.H, prob->H0, f.n));
+  } else if (p.init != NOMAD_INIT_HASH) {
+    std::vector<float> Hh(static_cast<size_t>(f.n) * f.dim);
+    RC(nomad_reference_init(0, f.n, f.dim, p.seed, p.init_parts, nullptr, Hh.data()));
+    RC(put_factor(c, f.H, Hh.data(), f.n));
+  }
+
+  // ---- rating sets ---------------------------------------------------------------
+  nomad::Csc train, test;
+  RC(nomad::build_csc(prob->train, f.m, f.n, train, threads));
+  RC(nomad::build_csc(prob->test, f.m, f.n, test, threads));
+  c->nnz_train = train.nnz();
+  c->nnz_test = test.nnz();
+  RC(upload_csc(c, train, &c->train, &c->train_ptr));
+  RC(upload_csc(c, test, &c->test, &c->test_ptr));
+  for (int32_t j = 0; j < f.n; ++j)
+    c->max_column = std::max<int64_t>(c->max_column, train.col_ptr[j + 1] - train.col_ptr[j]);
+
+  // ---- mode-specific layout --------------------------------------------------------
+  if (p.mode == NOMAD_MODE_ASYNC) {
+    c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 8) : 8;
+    const int nv = f.nvec <= 32 ? 1 : (f.nvec <= 64 ? 2 : 4);
+    int bps = 0;
+    CK(nomad::async_occupancy(f.bf16, nv, p.exact, c->wpb, f.kpad, &bps));
+    if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "async kernel does not fit on an SM");
+    if (p.blocks_per_sm > 0) bps = std::min(bps, p.blocks_per_sm);
+    const int64_t capacity = static_cast<int64_t>(bps) * c->num_sms * c->wpb;
+    c->P = static_cast<int32_t>(p.workers > 0 ? std::min<int64_t>(p.workers, capacity) : capacity);
+    c->grid = (c->P + c->wpb - 1) / c->wpb;
+    nomad::AsyncLayout L;
+    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, L, threads));
+    c->n_active = L.n_active;
+    c->n_segments = static_cast<int64_t>(L.segs.size());
+    RC(upload(c, &c->segs, reinterpret_cast<const int4*>(L.segs.data()), L.segs.size()));
+    RC(upload(c, &c->vl_ptr, L.vl_ptr.data(), L.vl_ptr.size()));
+    RC(upload(c, &c->qnext0, L.qnext0.data(), L.qnext0.size()));
+    RC(upload(c, &c->qtail0, L.qtail0.data(), L.qtail0.size()));
+    RC(dalloc(c, &c->qnext, L.qnext0.size()));
+    RC(dalloc(c, &c->qtail, L.qtail0.size()));
+    RC(dalloc(c, &c->tok_pos, f.n));
+    RC(dalloc(c, &c->tok_epoch, f.n));
+    RC(dalloc(c, &c->ctrl, 4));
+    RC(dalloc(c, &c->progress, 1));
+    RC(dalloc(c, &c->stats, 4));
+    RC(dalloc(c, &c->err_sum, 1));
+    RC(reset_tokens(c));
+  } else if (p.mode == NOMAD_MODE_DSGD) {
+    c->innerB = p.dsgd_inner_blocks > 0 ? p.dsgd_inner_blocks : 2 * c->num_sms * 4;
+    nomad::DsgdLayout D;
+    RC(nomad::build_dsgd_layout(prob->train, f.m, f.n, c->innerB, D));
+    RC(upload(c, &c->blk_ptr, D.blk_ptr.data(), D.blk_ptr.size()));
+    RC(upload(c, &c->rates, reinterpret_cast<const int4*>(D.rates.data()), D.rates.size() / 4));
+    RC(dalloc(c, &c->sched, static_cast<size_t>(c->innerB) * c->innerB));
+  } else if (p.mode == NOMAD_MODE_REPLAY) {
+    c->P = 1;
+  } else {
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown mode %d", p.mode);
+  }
+  if (!c->err_sum) RC(dalloc(c, &c->err_sum, 1));
+  c->sse_grid = c->num_sms * 8;
+  RC(dalloc(c, &c->partials, c->sse_grid));
+  RC(dalloc(c, &c->sse_out, 2));
+  RC(ensure_steps(c, 64));
+  CK(cudaStreamSynchronize(c->stream));
+  return NOMAD_OK;
+}
+
+int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
+  const int32_t n = c->f.n;
+  const size_t qn = static_cast<size_t>(n) + c->P;
+  if (c->prm.debug_flags & 1) {
+    CK(nomad::launch_empty_queues(c->qnext, c->qtail, n, c->P, c->stream));
+  } else {
+    CK(cudaMemcpyAsync(c->qnext, c->qnext0, qn * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->qtail, c->qtail0, c->P * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CK(cudaMemsetAsync(c->ctrl, 0, 4 * sizeof(int32_t), c->stream));
+  CK(cudaMemsetAsync(c->progress, 0, sizeof(unsigned long long), c->stream));
+  CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->stream));
+  CK(cudaMemsetAsync(c->err_sum, 0, sizeof(double), c->stream));
+  nomad::AsyncArgs a;
+  a.f = c->f;
+  a.ratings = c->train;
+  a.segs = c->segs;
+  a.vl_ptr = c->vl_ptr;
+  a.tok_pos = c->tok_pos;
+  a.tok_epoch = c->tok_epoch;
+  a.steps = c->steps;
+  a.n_steps = c->n_steps;
+  a.qnext = c->qnext;
+  a.qtail = c->qtail;
+  a.ctrl = c->ctrl;
+  a.progress = c->progress;
+  a.stats = c->stats;
+  a.err_sum = c->err_sum;
+  a.P = c->P;
+  a.n_active = c->n_active;
+  a.target_epoch = c->epochs_done + E;
+  a.lambda = static_cast<float>(c->prm.reg);
+  a.seed32 = static_cast<uint32_t>(c->prm.seed ^ (c->prm.seed >> 32));
+  a.budget_ns = static_cast<int64_t>(std::max(c->prm.spin_budget_ms, 1)) * 1000000LL;
+  a.exact = c->prm.exact;
+  a.warps_per_block = c->wpb;
+  a.grid = c->grid;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  if (c->n_active > 0) CK(nomad::launch_async(a, c->stream));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  int32_t ctrl[4];
+  unsigned long long stats[4];
+  double esum = 0;
+  CK(cudaMemcpy(ctrl, c->ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(stats, c->stats, sizeof(stats), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&esum, c->err_sum, sizeof(double), cudaMemcpyDeviceToHost));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (st) {
+    st->updates = static_cast<int64_t>(stats[0]);
+    st->hops = static_cast<int64_t>(stats[1]);
+    st->failures = static_cast<int64_t>(stats[2]);
+    st->device_ms = ms;
+    st->online_sse = esum;
+  }
+  if (ctrl[1] != 0 || (c->n_active > 0 && ctrl[0] != c->n_active)) {
+    RC(reset_tokens(c));
+    if (ctrl[1] == 2) NOMAD_FAIL(NOMAD_ERR_BOUNDS, "device bounds check failed");
+    NOMAD_FAIL(NOMAD_ERR_TIMEOUT,
+               "async epoch stopped: %d of %d tokens finished, no progress for %d ms",
+               ctrl[0], c->n_active, c->prm.spin_budget_ms);
+  }
+  return NOMAD_OK;
+}
+
+int epoch_replay(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
+  CK(cudaMemsetAsync(c->err_sum, 0, sizeof(double), c->stream));
+  nomad::ReplayArgs a;
+  a.f = c->f;
+  a.ratings = c->train;
+  a.col_ptr = c->train_ptr;
+  a.steps = c->steps;
+  a.first_epoch = c->epochs_done;
+  a.n_epochs = E;
+  a.lambda = static_cast<float>(c->prm.reg);
+  a.seed32 = static_cast<uint32_t>(c->prm.seed ^ (c->prm.seed >> 32));
+  a.err_sum = c->err_sum;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(nomad::launch_replay(a, c->stream));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  double esum = 0;
+  CK(cudaMemcpy(&esum, c->err_sum, sizeof(double), cudaMemcpyDeviceToHost));
+  if (st) {
+    st->updates = c->nnz_train * E;
+    st->hops = static_cast<int64_t>(c->f.n) * E;
+    st->device_ms = ms;
+    st->online_sse = esum;
+  }
+  return NOMAD_OK;
+}
+
+int epoch_dsgd(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
+  nomad::DsgdArgs a;
+  a.f = c->f;
+  a.rates = c->rates;
+  a.blk_ptr = c->blk_ptr;
+  a.sched = c->sched;
+  a.innerB = c->innerB;
+  a.lambda = static_cast<float>(c->prm.reg);
+  a.seed32 = static_cast<uint32_t>(c->prm.seed ^ (c->prm.seed >> 32));
+  a.exact = c->prm.exact;
+  std::vector<int32_t> sched;
+  float total_ms = 0;
+  for (int32_t k = 0; k < E; ++k) {
+    const int32_t iter = c->epochs_done + k + 1;
+    nomad::dsgd_schedule(c->innerB, iter, c->prm.dsgd_strategy, sched);
+    CK(cudaMemcpyAsync(c->sched, sched.data(), sched.size() * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, c->stream));
+    // FIXED schedule of dsgd_mpi (sgd-mpi-omp.cpp:308-309), lrate/decay in double
+    a.step = static_cast<float>(1.5 * c->prm.lrate / (1.0 + c->prm.drate * std::pow(iter, 1.5)));
+    a.iter = iter;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int32_t s = 0; s < c->innerB; ++s) CK(nomad::launch_dsgd_stratum(a, s, c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    total_ms += ms;
+  }
+  if (st) {
+    st->updates = c->nnz_train * E;
+    st->device_ms = total_ms;
+  }
+  return NOMAD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nomad_gpu_params_default(nomad_gpu_params* p) {
+  if (!p) return NOMAD_ERR_INVALID_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->struct_size = sizeof(*p);
+  // NomadOption defaults (Code/nomad/nomad_option.cpp:18-47)
+  p->dim = 100;
+  p->lrate = 0.001;
+  p->drate = 0.1;
+  p->reg = 1.0;
+  p->seed = 12345;
+  p->mode = NOMAD_MODE_ASYNC;
+  p->precision = NOMAD_PREC_FP32;
+  p->init = NOMAD_INIT_REFERENCE;
+  p->init_parts = 1;
+  p->balance = 1;
+  p->spin_budget_ms = 2000;
+  return NOMAD_OK;
+}
+
+int nomad_gpu_init(nomad_gpu_ctx** out, const nomad_gpu_problem* prob,
+                   const nomad_gpu_params* params) {
+  nomad::clear_last_error();
+  if (!out || !prob || !params) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (params->struct_size != static_cast<int32_t>(sizeof(nomad_gpu_params)))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "params.struct_size %d != %zu (ABI mismatch)",
+               params->struct_size, sizeof(nomad_gpu_params));
+  if (prob->m < 0 || prob->n < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "negative matrix size");
+  if (params->dim <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "dim must be positive");
+  if (params->init_parts <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "init_parts must be positive");
+  if (params->precision != NOMAD_PREC_FP32 && params->precision != NOMAD_PREC_BF16_SR)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown precision %d", params->precision);
+  if (!(params->lrate >= 0) || !(params->drate >= 0) || !(params->reg >= 0))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "lrate, drate and reg must be non-negative");
+  std::unique_ptr<nomad_gpu_ctx> c(new nomad_gpu_ctx());
+  c->prm = *params;
+  if (c->prm.mode == NOMAD_MODE_REPLAY) c->prm.exact = 1;
+  c->device = params->device;
+  int rc = init_impl(c.get(), prob);
+  if (rc) {
+    std::string msg = nomad::last_error();
+    nomad_gpu_destroy(c.release());
+    nomad::set_last_error("%s", msg.c_str());
+    return rc;
+  }
+  *out = c.release();
+  return NOMAD_OK;
+}
+
+int nomad_gpu_epoch(nomad_gpu_ctx* c, int32_t n_epochs, nomad_gpu_epoch_stats* st) {
+  nomad::clear_last_error();
+  if (!c || n_epochs < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
+  if (st) std::memset(st, 0, sizeof(*st));
+  const auto t0 = std::chrono::steady_clock::now();
+  CK(cudaSetDevice(c->device));
+  int rc = NOMAD_OK;
+  if (n_epochs > 0) {
+    RC(ensure_steps(c, c->epochs_done + n_epochs + 1));
+    if (c->prm.mode == NOMAD_MODE_ASYNC)
+      rc = epoch_async(c, n_epochs, st);
+    else if (c->prm.mode == NOMAD_MODE_REPLAY)
+      rc = epoch_replay(c, n_epochs, st);
+    else
+      rc = epoch_dsgd(c, n_epochs, st);
+    if (rc == NOMAD_OK) c->epochs_done += n_epochs;
+  }
+  if (st) {
+    st->epochs_done = c->epochs_done;
+    st->host_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
+int nomad_gpu_sse(nomad_gpu_ctx* c, double* train_sse, int64_t* train_count, double* test_sse,
+                  int64_t* test_count) {
+  nomad::clear_last_error();
+  if (!c) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null context");
+  CK(cudaSetDevice(c->device));
+  nomad::SseArgs a;
+  a.f = c->f;
+  a.partials = c->partials;
+  a.grid = c->sse_grid;
+  a.ratings = c->train;
+  a.col_ptr = c->train_ptr;
+  a.nnz = c->nnz_train;
+  a.out = c->sse_out;
+  CK(nomad::launch_sse(a, c->stream));
+  a.ratings = c->test;
+  a.col_ptr = c->test_ptr;
+  a.nnz = c->nnz_test;
+  a.out = c->sse_out + 1;
+  CK(nomad::launch_sse(a, c->stream));
+  double h[2];
+  CK(cudaMemcpyAsync(h, c->sse_out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (train_sse) *train_sse = h[0];
+  if (test_sse) *test_sse = h[1];
+  if (train_count) *train_count = c->nnz_train;
+  if (test_count) *test_count = c->nnz_test;
+  return NOMAD_OK;
+}
+
+int nomad_gpu_rmse(nomad_gpu_ctx* c, double* train_rmse, double* test_rmse) {
+  double s0 = 0, s1 = 0;
+  int64_t c0 = 0, c1 = 0;
+  int rc = nomad_gpu_sse(c, &s0, &c0, &s1, &c1);
+  if (rc) return rc;
+  if (train_rmse) *train_rmse = c0 ? std::sqrt(s0 / c0) : NAN;
+  if (test_rmse) *test_rmse = c1 ? std::sqrt(s1 / c1) : NAN;
+  return NOMAD_OK;
+}
+
+int nomad_gpu_get_factors(nomad_gpu_ctx* c, float* W, float* H) {
+  nomad::clear_last_error();
+  if (!c) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null context");
+  CK(cudaSetDevice(c->device));
+  if (W) RC(get_factor(c, c->f.W, W, c->f.m));
+  if (H) RC(get_factor(c, c->f.H, H, c->f.n));
+  return NOMAD_OK;
+}
+
+int nomad_gpu_set_factors(nomad_gpu_ctx* c, const float* W, const float* H) {
+  nomad::clear_last_error();
+  if (!c) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null context");
+  CK(cudaSetDevice(c->device));
+  if (W) RC(put_factor(c, c->f.W, W, c->f.m));
+  if (H) RC(put_factor(c, c->f.H, H, c->f.n));
+  return NOMAD_OK;
+}
+
+int nomad_gpu_get_info(nomad_gpu_ctx* c, nomad_gpu_info* info) {
+  if (!c || !info) return NOMAD_ERR_INVALID_ARG;
+  std::memset(info, 0, sizeof(*info));
+  info->m = c->f.m;
+  info->n = c->f.n;
+  info->dim = c->f.dim;
+  info->dim_padded = c->f.kpad;
+  info->nnz_train = c->nnz_train;
+  info->nnz_test = c->nnz_test;
+  info->workers = c->P;
+  info->active_tokens = c->n_active;
+  info->segments = c->n_segments;
+  info->max_column = c->max_column;
+  info->grid_blocks = c->grid;
+  info->block_threads = c->wpb * 32;
+  info->num_sms = c->num_sms;
+  info->inner_blocks = c->innerB;
+  info->device_bytes = c->device_bytes;
+  info->mode = c->prm.mode;
+  info->precision = c->prm.precision;
+  return NOMAD_OK;
+}
+
+void nomad_gpu_destroy(nomad_gpu_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* nomad_gpu_strerror(int status) {
+  switch (status) {
+    case NOMAD_OK: return "ok";
+    case NOMAD_ERR_INVALID_ARG: return "invalid argument";
+    case NOMAD_ERR_CUDA: return "CUDA runtime error";
+    case NOMAD_ERR_OOM: return "out of memory";
+    case NOMAD_ERR_TIMEOUT: return "device wait timed out";
+    case NOMAD_ERR_BOUNDS: return "device bounds check failed";
+    case NOMAD_ERR_IO: return "I/O error";
+    case NOMAD_ERR_FORMAT: return "not a train.dat/test.dat binary matrix";
+    case NOMAD_ERR_NO_DEVICE: return "no usable sm_103 device";
+    case NOMAD_ERR_UNSUPPORTED: return "unsupported option combination";
+    default: return "unknown status";
+  }
+}
+
+const char* nomad_gpu_last_error(void) { return nomad::last_error(); }
+
+int nomad_gpu_device_ok(int32_t device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return 0;
+  return prop.major * 10 + prop.minor == 103 ? 1 : 0;
+}
+
+}  // extern "C"

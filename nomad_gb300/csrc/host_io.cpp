@@ -1,0 +1,240 @@
+// host_io.cpp -- train.dat/test.dat I/O, the --output factor dump, the reference's
+// factor initialisation, and the library's host-side helpers.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <random>
+
+#include "common.h"
+
+namespace nomad {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_last_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+void clear_last_error() { g_last_error.clear(); }
+const char* last_error() { return g_last_error.c_str(); }
+
+int host_threads(int requested) {
+  if (requested > 0) return requested;
+  unsigned hw = std::thread::hardware_concurrency();
+  return hw ? static_cast<int>(hw) : 1;
+}
+
+void parallel_chunks(int64_t count, int threads,
+                     const std::function<void(int, int64_t, int64_t)>& fn) {
+  if (count <= 0) return;
+  threads = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(threads, count)));
+  if (threads == 1) {
+    fn(0, 0, count);
+    return;
+  }
+  std::vector<std::thread> pool;
+  pool.reserve(threads);
+  for (int t = 0; t < threads; ++t) {
+    const int64_t lo = count * t / threads, hi = count * (t + 1) / threads;
+    pool.emplace_back([&fn, t, lo, hi] { fn(t, lo, hi); });
+  }
+  for (auto& th : pool) th.join();
+}
+
+double SplitMix64::normal() {
+  // Box-Muller on two uniforms; u1 in (0, 1] so the log is finite.
+  const double u1 = 1.0 - uniform();
+  const double u2 = uniform();
+  return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+}
+
+}  // namespace nomad
+
+using nomad::set_last_error;
+
+extern "C" {
+
+// nb_data.cpp:32-78 -- header of the PETSc-style binary matrix, either id.
+int nomad_io_read_header(const char* path, int32_t* file_id, int32_t* m, int32_t* n,
+                         int64_t* nnz) {
+  nomad::clear_last_error();
+  if (!path) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null path");
+  std::ifstream f(path, std::ios::in | std::ios::binary);
+  if (!f) NOMAD_FAIL(NOMAD_ERR_IO, "cannot open file: %s", path);
+  int32_t id = 0;
+  if (!f.read(reinterpret_cast<char*>(&id), 4)) NOMAD_FAIL(NOMAD_ERR_FORMAT, "error in reading ID from %s", path);
+  int32_t mm = 0, nn = 0;
+  int64_t z = 0;
+  if (id == NOMAD_FILE_ID_INT) {
+    int32_t h[3];
+    if (!f.read(reinterpret_cast<char*>(h), sizeof(h))) NOMAD_FAIL(NOMAD_ERR_FORMAT, "error in reading header from %s", path);
+    mm = h[0];
+    nn = h[1];
+    z = h[2];
+  } else if (id == NOMAD_FILE_ID_LONG) {
+    int32_t h[2];
+    if (!f.read(reinterpret_cast<char*>(h), sizeof(h))) NOMAD_FAIL(NOMAD_ERR_FORMAT, "error in reading header from %s", path);
+    mm = h[0];
+    nn = h[1];
+    if (!f.read(reinterpret_cast<char*>(&z), sizeof(z))) NOMAD_FAIL(NOMAD_ERR_FORMAT, "error in reading nnz from %s", path);
+  } else {
+    NOMAD_FAIL(NOMAD_ERR_FORMAT, "%d does not identify a valid binary matrix file (%s)", id, path);
+  }
+  if (mm < 0 || nn < 0 || z < 0) NOMAD_FAIL(NOMAD_ERR_FORMAT, "negative sizes in header of %s", path);
+  if (file_id) *file_id = id;
+  if (m) *m = mm;
+  if (n) *n = nn;
+  if (nnz) *nnz = z;
+  return NOMAD_OK;
+}
+
+// nb_data.cpp:83-130 with one part: row counts, then every column index, then every
+// value.  Unlike the reference (which trusts the file) the counts and indices are
+// validated, and a short file is a NOMAD_ERR_FORMAT status rather than exit(1).
+int nomad_io_read(const char* path, nomad_io_matrix* out) {
+  if (!out) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null output");
+  std::memset(out, 0, sizeof(*out));
+  int32_t id, m, n;
+  int64_t nnz;
+  int rc = nomad_io_read_header(path, &id, &m, &n, &nnz);
+  if (rc) return rc;
+  std::ifstream f(path, std::ios::in | std::ios::binary);
+  f.seekg(id == NOMAD_FILE_ID_INT ? 16 : 20, std::ios::beg);
+  int32_t* rcnt = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
+  int32_t* cols = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+  double* vals = static_cast<double*>(std::malloc(sizeof(double) * std::max<int64_t>(nnz, 1)));
+  auto fail = [&](int code, const char* what) {
+    std::free(rcnt);
+    std::free(cols);
+    std::free(vals);
+    set_last_error("%s (%s)", what, path);
+    return code;
+  };
+  if (!rcnt || !cols || !vals) return fail(NOMAD_ERR_OOM, "host allocation failed");
+  if (!f.read(reinterpret_cast<char*>(rcnt), static_cast<std::streamsize>(m) * 4))
+    return fail(NOMAD_ERR_FORMAT, "error in reading nnz values from file");
+  int64_t total = 0;
+  for (int32_t i = 0; i < m; ++i) {
+    if (rcnt[i] < 0) return fail(NOMAD_ERR_FORMAT, "negative row count");
+    total += rcnt[i];
+  }
+  if (total != nnz) return fail(NOMAD_ERR_FORMAT, "row counts do not add up to nnz");
+  if (!f.read(reinterpret_cast<char*>(cols), static_cast<std::streamsize>(nnz) * 4))
+    return fail(NOMAD_ERR_FORMAT, "error in reading column indices from file");
+  if (!f.read(reinterpret_cast<char*>(vals), static_cast<std::streamsize>(nnz) * 8))
+    return fail(NOMAD_ERR_FORMAT, "error in reading matrix values from file");
+  for (int64_t i = 0; i < nnz; ++i)
+    if (cols[i] < 0 || cols[i] >= n) return fail(NOMAD_ERR_FORMAT, "column index out of range");
+  out->file_id = id;
+  out->m = m;
+  out->n = n;
+  out->nnz = nnz;
+  out->row_counts = rcnt;
+  out->cols = cols;
+  out->vals = vals;
+  return NOMAD_OK;
+}
+
+// convert.py:99-105 ("=iiii" header, then "=%si" row sizes, "=%si" indices,
+// "=%sd" values) and synthgen.cpp:298-311 (id 1015 with a long long nnz).
+int nomad_io_write(const char* path, int32_t m, int32_t n, int64_t nnz,
+                   const int32_t* row_counts, const int32_t* cols, const double* vals,
+                   int32_t file_id) {
+  nomad::clear_last_error();
+  if (!path || m < 0 || n < 0 || nnz < 0 || (m > 0 && !row_counts) ||
+      (nnz > 0 && (!cols || !vals)))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_io_write");
+  if (file_id == 0) file_id = nnz < (int64_t(1) << 31) ? NOMAD_FILE_ID_INT : NOMAD_FILE_ID_LONG;
+  if (file_id != NOMAD_FILE_ID_INT && file_id != NOMAD_FILE_ID_LONG)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown file id %d", file_id);
+  if (file_id == NOMAD_FILE_ID_INT && nnz >= (int64_t(1) << 31))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "nnz %lld does not fit the 1211216 header", (long long)nnz);
+  std::ofstream f(path, std::ios::out | std::ios::binary | std::ios::trunc);
+  if (!f) NOMAD_FAIL(NOMAD_ERR_IO, "cannot open %s for writing", path);
+  f.write(reinterpret_cast<const char*>(&file_id), 4);
+  f.write(reinterpret_cast<const char*>(&m), 4);
+  f.write(reinterpret_cast<const char*>(&n), 4);
+  if (file_id == NOMAD_FILE_ID_INT) {
+    const int32_t z = static_cast<int32_t>(nnz);
+    f.write(reinterpret_cast<const char*>(&z), 4);
+  } else {
+    const long long z = nnz;
+    f.write(reinterpret_cast<const char*>(&z), 8);
+  }
+  f.write(reinterpret_cast<const char*>(row_counts), static_cast<std::streamsize>(m) * 4);
+  f.write(reinterpret_cast<const char*>(cols), static_cast<std::streamsize>(nnz) * 4);
+  f.write(reinterpret_cast<const char*>(vals), static_cast<std::streamsize>(nnz) * 8);
+  if (!f) NOMAD_FAIL(NOMAD_ERR_IO, "short write to %s", path);
+  return NOMAD_OK;
+}
+
+void nomad_io_free(nomad_io_matrix* mat) {
+  if (!mat) return;
+  std::free(mat->row_counts);
+  std::free(mat->cols);
+  std::free(mat->vals);
+  std::memset(mat, 0, sizeof(*mat));
+}
+
+// nb_main.cpp:683-705 (rows) then :349-366 (columns); `ofs << "," << v` uses the
+// stream's default floatfield, i.e. %g with 6 significant digits.
+int nomad_io_write_factors(const char* path, int32_t m, int32_t n, int32_t dim,
+                           const float* W, const float* H) {
+  nomad::clear_last_error();
+  if (!path || dim <= 0 || (m > 0 && !W) || (n > 0 && !H))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_io_write_factors");
+  std::ofstream ofs(path, std::ios::out | std::ios::trunc);
+  if (!ofs) NOMAD_FAIL(NOMAD_ERR_IO, "cannot open %s for writing", path);
+  for (int32_t i = 0; i < m; ++i) {
+    ofs << "row," << i;
+    for (int32_t t = 0; t < dim; ++t) ofs << "," << static_cast<double>(W[int64_t(i) * dim + t]);
+    ofs << "\n";
+  }
+  for (int32_t j = 0; j < n; ++j) {
+    ofs << "column," << j;
+    for (int32_t t = 0; t < dim; ++t) ofs << "," << static_cast<double>(H[int64_t(j) * dim + t]);
+    ofs << "\n";
+  }
+  if (!ofs) NOMAD_FAIL(NOMAD_ERR_IO, "short write to %s", path);
+  return NOMAD_OK;
+}
+
+// nb_main.cpp:450-455 (rows of part t from mt19937_64(seed + rank*131 + t + 1)) and
+// nb_main.cpp:71-92 (every column's values from mt19937_64(seed + rank*131 + 139)),
+// single rank.  Row blocks follow read_data's ceil(m / parts) split (nb_data.cpp:83-89).
+int nomad_reference_init(int32_t m, int32_t n, int32_t dim, uint64_t seed,
+                         int32_t init_parts, float* W, float* H) {
+  nomad::clear_last_error();
+  if (m < 0 || n < 0 || dim <= 0 || init_parts <= 0)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_reference_init");
+  std::uniform_real_distribution<double> init_dist(0, 1.0 / std::sqrt(dim));
+  const int32_t P = init_parts;
+  const int32_t rows_per_part = m / P + ((m % P > 0) ? 1 : 0);
+  if (W) {
+    nomad::parallel_chunks(P, nomad::host_threads(), [&](int, int64_t lo_t, int64_t hi_t) {
+      for (int64_t t = lo_t; t < hi_t; ++t) {
+        const int64_t lo = std::min<int64_t>(int64_t(rows_per_part) * t, m);
+        const int64_t hi = std::min<int64_t>(int64_t(rows_per_part) * (t + 1), m);
+        std::mt19937_64 rng(seed + 0 * 131 + t + 1);
+        std::uniform_real_distribution<double> dist(0, 1.0 / std::sqrt(dim));
+        for (int64_t i = lo * dim; i < hi * dim; ++i) W[i] = static_cast<float>(dist(rng));
+      }
+    });
+  }
+  if (H) {
+    std::mt19937_64 rng(seed + 0 * 131 + 139);
+    for (int64_t i = 0; i < int64_t(n) * dim; ++i) H[i] = static_cast<float>(init_dist(rng));
+  }
+  return NOMAD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,310 @@
+// host_layout.cpp -- host-side construction of the device data layout: CSC by column,
+// worker row blocks, token visit lists, initial queues, DSGD blocks and schedules.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+
+#include "layout.h"
+
+namespace nomad {
+
+namespace {
+
+// Row-major view of a rating set: entries listed row by row.
+struct RowMajor {
+  std::vector<int64_t> row_ptr;  // [m+1]
+  const int32_t* cols = nullptr;
+  const double* v64 = nullptr;
+  const float* v32 = nullptr;
+  // storage when the input was COO and had to be reordered
+  std::vector<int32_t> own_cols;
+  std::vector<float> own_vals;
+  float val(int64_t i) const { return v64 ? static_cast<float>(v64[i]) : v32[i]; }
+};
+
+int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R) {
+  if (A.nnz < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "negative nnz");
+  if (A.nnz > 0 && (!A.cols || (!A.vals_f64 && !A.vals_f32)))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "rating set has nnz > 0 but null arrays");
+  if (A.vals_f64 && A.vals_f32) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "give vals_f64 or vals_f32, not both");
+  R.row_ptr.assign(static_cast<size_t>(m) + 1, 0);
+  if (A.row_counts) {
+    for (int32_t i = 0; i < m; ++i) {
+      if (A.row_counts[i] < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "negative row count at row %d", i);
+      R.row_ptr[i + 1] = R.row_ptr[i] + A.row_counts[i];
+    }
+    if (R.row_ptr[m] != A.nnz)
+      NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "row counts add up to %lld, nnz is %lld",
+                 (long long)R.row_ptr[m], (long long)A.nnz);
+    R.cols = A.cols;
+    R.v64 = A.vals_f64;
+    R.v32 = A.vals_f32;
+  } else if (A.nnz > 0) {
+    if (!A.rows) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "rating set needs row_counts or rows");
+    for (int64_t i = 0; i < A.nnz; ++i) {
+      const int32_t r = A.rows[i];
+      if (r < 0 || r >= m) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "row index %d out of range [0, %d)", r, m);
+      R.row_ptr[r + 1]++;
+    }
+    for (int32_t i = 0; i < m; ++i) R.row_ptr[i + 1] += R.row_ptr[i];
+    std::vector<int64_t> fill(R.row_ptr.begin(), R.row_ptr.end() - 1);
+    R.own_cols.resize(A.nnz);
+    R.own_vals.resize(A.nnz);
+    for (int64_t i = 0; i < A.nnz; ++i) {
+      const int64_t o = fill[A.rows[i]]++;
+      R.own_cols[o] = A.cols[i];
+      R.own_vals[o] = A.vals_f64 ? static_cast<float>(A.vals_f64[i]) : A.vals_f32[i];
+    }
+    R.cols = R.own_cols.data();
+    R.v32 = R.own_vals.data();
+  }
+  for (int64_t i = 0; i < A.nnz; ++i)
+    if (R.cols[i] < 0 || R.cols[i] >= n)
+      NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "column index %d out of range [0, %d)", R.cols[i], n);
+  return NOMAD_OK;
+}
+
+// glibc's rand() stream (srand seeds the TYPE_3 additive generator; initstate_r with a
+// 128-byte state does the same) kept private so the process-global state is untouched.
+struct GlibcRand {
+  struct random_data data {};
+  char state[128];
+  explicit GlibcRand(unsigned seed) {
+    std::memset(state, 0, sizeof(state));
+    data.state = nullptr;
+    initstate_r(seed, state, sizeof(state), &data);
+  }
+  int next() {
+    int32_t r;
+    random_r(&data, &r);
+    return r;
+  }
+};
+
+}  // namespace
+
+float step_size_f32(double lrate, double drate, int32_t cnt) {
+  const float learn_rate = static_cast<float>(lrate);
+  const float decay_rate = static_cast<float>(drate);
+  return static_cast<float>(learn_rate * 1.5 / (1.0 + decay_rate * std::pow(cnt + 1, 1.5)));
+}
+
+int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int threads) {
+  RowMajor R;
+  int rc = to_row_major(A, m, n, R);
+  if (rc) return rc;
+  const int64_t nnz = A.nnz;
+  out.m = m;
+  out.n = n;
+  out.col_ptr.assign(static_cast<size_t>(n) + 1, 0);
+  out.ratings.resize(static_cast<size_t>(nnz));
+  if (nnz == 0) return NOMAD_OK;
+  // Stable counting sort by column: contiguous chunks of the row-major entries, one
+  // column histogram per chunk, then each chunk scatters in order.
+  const int T = std::max<int>(1, std::min<int64_t>(threads, std::max<int64_t>(1, nnz / 65536)));
+  std::vector<std::vector<int64_t>> hist(T, std::vector<int64_t>(n, 0));
+  parallel_chunks(nnz, T, [&](int t, int64_t lo, int64_t hi) {
+    std::vector<int64_t>& h = hist[t];
+    for (int64_t i = lo; i < hi; ++i) h[R.cols[i]]++;
+  });
+  for (int32_t j = 0; j < n; ++j) {
+    int64_t s = 0;
+    for (int t = 0; t < T; ++t) s += hist[t][j];
+    out.col_ptr[j + 1] = out.col_ptr[j] + s;
+  }
+  for (int32_t j = 0; j < n; ++j) {  // hist[t][j] becomes chunk t's write cursor
+    int64_t pos = out.col_ptr[j];
+    for (int t = 0; t < T; ++t) {
+      const int64_t c = hist[t][j];
+      hist[t][j] = pos;
+      pos += c;
+    }
+  }
+  parallel_chunks(nnz, T, [&](int t, int64_t lo, int64_t hi) {
+    std::vector<int64_t>& cur = hist[t];
+    int32_t r = static_cast<int32_t>(std::upper_bound(R.row_ptr.begin(), R.row_ptr.end(), lo) -
+                                     R.row_ptr.begin()) - 1;
+    for (int64_t i = lo; i < hi; ++i) {
+      while (R.row_ptr[r + 1] <= i) ++r;
+      out.ratings[cur[R.cols[i]]++] = Rating{r, R.val(i)};
+    }
+  });
+  // repeated cells would break the distinct-rows property a column visit relies on
+  std::atomic<int64_t> dup{-1};
+  parallel_chunks(n, threads, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t j = lo; j < hi && dup.load(std::memory_order_relaxed) < 0; ++j)
+      for (int64_t o = out.col_ptr[j] + 1; o < out.col_ptr[j + 1]; ++o)
+        if (out.ratings[o].row == out.ratings[o - 1].row) {
+          dup.store(j);
+          break;
+        }
+  });
+  if (dup.load() >= 0)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "repeated (row, column) cell in column %lld", (long long)dup.load());
+  return NOMAD_OK;
+}
+
+int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
+                       AsyncLayout& L, int threads) {
+  const int32_t m = csc.m, n = csc.n;
+  const int64_t nnz = csc.nnz();
+  if (P <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker count must be positive");
+  L.P = P;
+  L.row_start.assign(static_cast<size_t>(P) + 1, m);
+  if (balance == 0 || nnz == 0) {
+    // read_data's split: ceil(m/P) rows per worker (nb_data.cpp:83-89)
+    const int64_t per = m / P + ((m % P > 0) ? 1 : 0);
+    for (int32_t w = 0; w <= P; ++w) L.row_start[w] = static_cast<int32_t>(std::min<int64_t>(per * w, m));
+  } else {
+    // contiguous blocks holding ~nnz/P ratings each
+    std::vector<int32_t> row_nnz(m, 0);
+    parallel_chunks(nnz, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t o = lo; o < hi; ++o)
+        __atomic_fetch_add(&row_nnz[csc.ratings[o].row], 1, __ATOMIC_RELAXED);
+    });
+    int64_t acc = 0;
+    int32_t w = 1;
+    L.row_start[0] = 0;
+    for (int32_t i = 0; i < m && w < P; ++i) {
+      acc += row_nnz[i];
+      while (w < P && acc >= (nnz * w + P - 1) / P) L.row_start[w++] = i + 1;
+    }
+    for (; w <= P; ++w) L.row_start[w] = m;
+  }
+  // visit lists: the rows of a column are ascending, so each worker's share is a run
+  L.vl_ptr.assign(static_cast<size_t>(n) + 1, 0);
+  auto worker_of = [&](int32_t row) {
+    return static_cast<int32_t>(std::upper_bound(L.row_start.begin(), L.row_start.end(), row) -
+                                L.row_start.begin()) - 1;
+  };
+  std::vector<int64_t> nseg(n, 0);
+  parallel_chunks(n, threads, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t j = lo; j < hi; ++j) {
+      int64_t c = 0;
+      int32_t w = -1, wend = 0;
+      for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
+        const int32_t r = csc.ratings[o].row;
+        if (w < 0 || r >= wend) {
+          w = worker_of(r);
+          wend = L.row_start[w + 1];
+          ++c;
+        }
+      }
+      nseg[j] = c;
+    }
+  });
+  for (int32_t j = 0; j < n; ++j) L.vl_ptr[j + 1] = L.vl_ptr[j] + nseg[j];
+  L.segs.resize(static_cast<size_t>(L.vl_ptr[n]));
+  std::vector<int64_t> maxseg(std::max(threads, 1), 0);
+  parallel_chunks(n, threads, [&](int t, int64_t lo, int64_t hi) {
+    for (int64_t j = lo; j < hi; ++j) {
+      Segment* s = L.segs.data() + L.vl_ptr[j];
+      int64_t c = -1;
+      int32_t w = -1, wend = 0;
+      for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
+        const int32_t r = csc.ratings[o].row;
+        if (w < 0 || r >= wend) {
+          w = worker_of(r);
+          wend = L.row_start[w + 1];
+          ++c;
+          s[c] = Segment{o, 0, w};
+        }
+        s[c].len++;
+      }
+      const int64_t k = nseg[j];
+      for (int64_t i = 0; i < k; ++i) maxseg[t] = std::max<int64_t>(maxseg[t], s[i].len);
+      // the token's route: a seeded random order of its visits (pool.cpp:32-38 draws
+      // a random permutation of the workers; empty visits are skipped here)
+      SplitMix64 rng(stream_key(seed, 137, static_cast<uint64_t>(j)));
+      for (int64_t i = k - 1; i > 0; --i) std::swap(s[i], s[rng.below(i + 1)]);
+    }
+  });
+  L.max_segment = *std::max_element(maxseg.begin(), maxseg.end());
+  L.max_column = 0;
+  L.n_active = 0;
+  for (int32_t j = 0; j < n; ++j) {
+    L.max_column = std::max<int64_t>(L.max_column, csc.col_ptr[j + 1] - csc.col_ptr[j]);
+    if (nseg[j] > 0) ++L.n_active;
+  }
+  // initial queues: every active token at its first worker, in column order
+  // (nb_main.cpp:82-97 pushes the tokens in index order)
+  L.qnext0.assign(static_cast<size_t>(n) + P, -1);
+  L.qtail0.resize(P);
+  for (int32_t w = 0; w < P; ++w) L.qtail0[w] = n + w;
+  for (int32_t j = 0; j < n; ++j) {
+    if (nseg[j] == 0) continue;
+    const int32_t w = L.segs[L.vl_ptr[j]].worker;
+    L.qnext0[L.qtail0[w]] = j;
+    L.qtail0[w] = j;
+  }
+  return NOMAD_OK;
+}
+
+int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
+                      DsgdLayout& D) {
+  RowMajor R;
+  int rc = to_row_major(A, m, n, R);
+  if (rc) return rc;
+  if (innerB <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "DSGD needs innerB > 0");
+  D.innerB = innerB;
+  D.innerBm = m / innerB + ((m % innerB) ? 1 : 0);
+  D.innerBn = n / innerB + ((n % innerB) ? 1 : 0);
+  if (D.innerBm == 0) D.innerBm = 1;
+  if (D.innerBn == 0) D.innerBn = 1;
+  const int64_t nb = static_cast<int64_t>(innerB) * innerB;
+  const int64_t nnz = A.nnz;
+  D.blk_ptr.assign(static_cast<size_t>(nb) + 1, 0);
+  auto bid_of = [&](int32_t r, int32_t c) {
+    return static_cast<int64_t>(r / D.innerBm) * innerB + c / D.innerBn;
+  };
+  for (int32_t r = 0; r < m; ++r)
+    for (int64_t i = R.row_ptr[r]; i < R.row_ptr[r + 1]; ++i) D.blk_ptr[bid_of(r, R.cols[i]) + 1]++;
+  for (int64_t b = 0; b < nb; ++b) D.blk_ptr[b + 1] += D.blk_ptr[b];
+  D.rates.resize(static_cast<size_t>(nnz) * 4);
+  std::vector<int64_t> fill(D.blk_ptr.begin() + 1, D.blk_ptr.end());  // fill backwards
+  for (int32_t r = 0; r < m; ++r)
+    for (int64_t i = R.row_ptr[r]; i < R.row_ptr[r + 1]; ++i) {
+      const int64_t o = --fill[bid_of(r, R.cols[i])];
+      const float v = R.val(i);
+      int32_t bits;
+      std::memcpy(&bits, &v, 4);
+      D.rates[o * 4 + 0] = r;
+      D.rates[o * 4 + 1] = R.cols[i];
+      D.rates[o * 4 + 2] = bits;
+      D.rates[o * 4 + 3] = 0;
+    }
+  return NOMAD_OK;
+}
+
+void dsgd_schedule(int32_t innerB, int32_t iter, int32_t strategy, std::vector<int32_t>& out) {
+  // inner_perm / inner_offset persist across iterations and are reshuffled under
+  // WOR_STRATUM after srand(34586 + iter) (sgd-mpi-omp.cpp:290-352); with B = 1 the
+  // outer shuffles draw nothing.  Shuffle = libstdc++ random_shuffle: for i = 1..N-1
+  // swap a[i] with a[rand() % (i+1)].
+  std::vector<int32_t> perm(innerB), offset(innerB), cur(innerB);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::iota(offset.begin(), offset.end(), 0);
+  auto shuffle = [](std::vector<int32_t>& a, GlibcRand& g) {
+    for (size_t i = 1; i < a.size(); ++i) {
+      const size_t j = static_cast<size_t>(g.next()) % (i + 1);
+      if (i != j) std::swap(a[i], a[j]);
+    }
+  };
+  for (int32_t it = 1; it <= iter; ++it) {
+    GlibcRand g(34586u + static_cast<unsigned>(it));
+    if (strategy == 2) {
+      shuffle(perm, g);
+      shuffle(offset, g);
+    }
+  }
+  out.assign(static_cast<size_t>(innerB) * innerB, 0);
+  for (int32_t i = 0; i < innerB; ++i) {
+    for (int32_t ii = 0; ii < innerB; ++ii) cur[perm[ii]] = (ii + offset[i]) % innerB;
+    for (int32_t bi = 0; bi < innerB; ++bi) out[static_cast<size_t>(i) * innerB + bi] = cur[bi];
+  }
+}
+
+}  // namespace nomad

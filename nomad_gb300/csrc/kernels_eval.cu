@@ -1,0 +1,248 @@
+// kernels_eval.cu -- evaluation (squared-error sums with FP64 accumulation), factor
+// initialisation and layout-conversion kernels for sm_103a.
+#include <cuda_bf16.h>
+
+#include "device_common.cuh"
+#include "launch.h"
+
+namespace {
+
+using nd::kFull;
+using nd::Vec;
+
+template <typename Store>
+__device__ __forceinline__ float dot_vec(const Store* a, const Store* b, int v);
+template <>
+__device__ __forceinline__ float dot_vec<float>(const float* a, const float* b, int v) {
+  const float4 x = reinterpret_cast<const float4*>(a)[v];
+  const float4 y = __ldcg(reinterpret_cast<const float4*>(b) + v);
+  return fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, x.w * y.w)));
+}
+template <>
+__device__ __forceinline__ float dot_vec<__nv_bfloat16>(const __nv_bfloat16* a, const __nv_bfloat16* b, int v) {
+  float x[8], y[8];
+  nd::load_vec<__nv_bfloat16>(a, v, x);
+  nd::load_vec_cg<__nv_bfloat16>(b, v, y);
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s = fmaf(x[i], y[i], s);
+  return s;
+}
+
+// Squared-error sum over a CSC rating set (the evaluation pass of
+// Code/nomad/nb_main.cpp:617-653): e = <h_j, w_i> - v in fp32, e*e summed in FP64.
+// A warp takes 32 consecutive ratings; the column of the first one is found by a
+// binary search of col_ptr and every lane walks forward to its own column.  The
+// warp then evaluates the 32 ratings one by one (lanes across the row), loading four
+// ratings' rows at a time.  Each block writes one FP64 partial; a single-block pass
+// adds the partials in a fixed order, so the result is deterministic.
+template <typename Store>
+__global__ void __launch_bounds__(256) sse_kernel(nomad::SseArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int warps = blockDim.x >> 5;
+  const Store* __restrict__ W = static_cast<const Store*>(a.f.W);
+  const Store* __restrict__ H = static_cast<const Store*>(a.f.H);
+  const int n = a.f.n;
+  const int64_t nchunks = (a.nnz + 31) / 32;
+  double acc = 0.0;
+  for (int64_t c = static_cast<int64_t>(blockIdx.x) * warps + wib; c < nchunks;
+       c += static_cast<int64_t>(gridDim.x) * warps) {
+    const int64_t base = c * 32;
+    const int cnt = static_cast<int>(a.nnz - base < 32 ? a.nnz - base : 32);
+    const int64_t idx = base + lane;
+    int j = 0;
+    if (lane == 0) {  // largest j with col_ptr[j] <= base
+      int lo = 0, hi = n;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a.col_ptr[mid]) <= base) lo = mid; else hi = mid;
+      }
+      j = lo;
+    }
+    j = __shfl_sync(kFull, j, 0);
+    int2 rv = make_int2(0, 0);
+    if (lane < cnt) {
+      rv = __ldg(&a.ratings[idx]);
+      while (__ldg(&a.col_ptr[j + 1]) <= idx) ++j;
+    }
+    float my_err = 0.f;
+    for (int t0 = 0; t0 < cnt; t0 += 4) {
+      float part[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u;
+        const int r = __shfl_sync(kFull, rv.x, t & 31);
+        const int jj = __shfl_sync(kFull, j, t & 31);
+        part[u] = 0.f;
+        if (t < cnt) {
+          for (int v = lane; v < a.f.nvec; v += 32)
+            part[u] += dot_vec<Store>(W + static_cast<int64_t>(r) * a.f.kpad,
+                                      H + static_cast<int64_t>(jj) * a.f.kpad, v);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float d = nd::warp_allreduce(part[u], 32);
+        if (lane == t0 + u) my_err = d - __int_as_float(rv.y);
+      }
+    }
+    if (lane < cnt) acc += static_cast<double>(my_err * my_err);
+  }
+  // block reduction in a fixed order
+  for (int s = 16; s >= 1; s >>= 1) acc += __shfl_xor_sync(kFull, acc, s);
+  __shared__ double red[32];
+  if (lane == 0) red[wib] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < warps; ++i) s += red[i];
+    a.partials[blockIdx.x] = s;
+  }
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ partials, int count, double* out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) s += partials[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w >= 1; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// U(0, 1/sqrt(dim)) factors from a counter hash of (seed, row, element); padding 0.
+template <typename Store>
+__global__ void init_hash_kernel(Store* __restrict__ X, int64_t rows, int dim, int kpad,
+                                 uint32_t seed, float scale) {
+  const int64_t total = rows * kpad;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / kpad;
+    const int k = static_cast<int>(i - r * kpad);
+    float v = 0.f;
+    if (k < dim) {
+      const uint32_t h = nd::hash32(seed ^ nd::hash32(static_cast<uint32_t>(r) ^
+                                                      nd::hash32(static_cast<uint32_t>(r >> 32) + k * 0x9E3779B9u)));
+      v = static_cast<float>(h >> 8) * (1.0f / 16777216.0f) * scale;
+    }
+    if (sizeof(Store) == 4)
+      reinterpret_cast<float*>(X)[i] = v;
+    else
+      reinterpret_cast<__nv_bfloat16*>(X)[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// Dense [rows x dim] fp32 <-> padded [rows x kpad] storage (bf16: round to nearest).
+template <typename Store>
+__global__ void f32_to_store_kernel(const float* __restrict__ src, Store* __restrict__ dst,
+                                    int64_t rows, int dim, int kpad) {
+  const int64_t total = rows * kpad;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / kpad;
+    const int k = static_cast<int>(i - r * kpad);
+    const float v = k < dim ? src[r * dim + k] : 0.f;
+    if (sizeof(Store) == 4)
+      reinterpret_cast<float*>(dst)[i] = v;
+    else
+      reinterpret_cast<__nv_bfloat16*>(dst)[i] = __float2bfloat16_rn(v);
+  }
+}
+template <typename Store>
+__global__ void store_to_f32_kernel(const Store* __restrict__ src, float* __restrict__ dst,
+                                    int64_t rows, int dim, int kpad) {
+  const int64_t total = rows * dim;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / dim;
+    const int k = static_cast<int>(i - r * dim);
+    if (sizeof(Store) == 4)
+      dst[i] = reinterpret_cast<const float*>(src)[r * kpad + k];
+    else
+      dst[i] = __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(src)[r * kpad + k]);
+  }
+}
+
+__global__ void empty_queues_kernel(int32_t* qnext, int32_t* qtail, int32_t n, int32_t P) {
+  const int64_t total = static_cast<int64_t>(n) + P;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    qnext[i] = -1;
+    if (i >= n) qtail[i - n] = static_cast<int32_t>(i);
+  }
+}
+
+int grid_for(int64_t work) {
+  const int64_t g = (work + 255) / 256;
+  return static_cast<int>(g < 1 ? 1 : (g > 152 * 32 ? 152 * 32 : g));
+}
+
+}  // namespace
+
+namespace nomad {
+
+cudaError_t launch_sse(const SseArgs& a, cudaStream_t s) {
+  if (a.nnz == 0) return cudaMemsetAsync(a.out, 0, sizeof(double), s);
+  if (a.f.bf16)
+    sse_kernel<__nv_bfloat16><<<a.grid, 256, 0, s>>>(a);
+  else
+    sse_kernel<float><<<a.grid, 256, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_partials_kernel<<<1, 256, 0, s>>>(a.partials, a.grid, a.out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_hash(const DevFactors& f, uint64_t seed, cudaStream_t s) {
+  const float scale = 1.0f / sqrtf(static_cast<float>(f.dim));
+  const uint32_t s1 = static_cast<uint32_t>(seed * 0x9E3779B97F4A7C15ULL >> 32);
+  const uint32_t s2 = (s1 ^ 0x68E31DA4u) * 0x1B873593u;
+  if (f.bf16) {
+    init_hash_kernel<__nv_bfloat16><<<grid_for(int64_t(f.m) * f.kpad), 256, 0, s>>>(
+        static_cast<__nv_bfloat16*>(f.W), f.m, f.dim, f.kpad, s1, scale);
+    init_hash_kernel<__nv_bfloat16><<<grid_for(int64_t(f.n) * f.kpad), 256, 0, s>>>(
+        static_cast<__nv_bfloat16*>(f.H), f.n, f.dim, f.kpad, s2, scale);
+  } else {
+    init_hash_kernel<float><<<grid_for(int64_t(f.m) * f.kpad), 256, 0, s>>>(
+        static_cast<float*>(f.W), f.m, f.dim, f.kpad, s1, scale);
+    init_hash_kernel<float><<<grid_for(int64_t(f.n) * f.kpad), 256, 0, s>>>(
+        static_cast<float*>(f.H), f.n, f.dim, f.kpad, s2, scale);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_store(const float* src, void* dst, int64_t rows, int32_t dim,
+                                int32_t kpad, int bf16, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  if (bf16)
+    f32_to_store_kernel<__nv_bfloat16><<<grid_for(rows * kpad), 256, 0, s>>>(
+        src, static_cast<__nv_bfloat16*>(dst), rows, dim, kpad);
+  else
+    f32_to_store_kernel<float><<<grid_for(rows * kpad), 256, 0, s>>>(src, static_cast<float*>(dst),
+                                                                     rows, dim, kpad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_store_to_f32(const void* src, float* dst, int64_t rows, int32_t dim,
+                                int32_t kpad, int bf16, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  if (bf16)
+    store_to_f32_kernel<__nv_bfloat16><<<grid_for(rows * dim), 256, 0, s>>>(
+        static_cast<const __nv_bfloat16*>(src), dst, rows, dim, kpad);
+  else
+    store_to_f32_kernel<float><<<grid_for(rows * dim), 256, 0, s>>>(static_cast<const float*>(src),
+                                                                    dst, rows, dim, kpad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_empty_queues(int32_t* qnext, int32_t* qtail, int32_t n, int32_t P,
+                                cudaStream_t s) {
+  empty_queues_kernel<<<grid_for(int64_t(n) + P), 256, 0, s>>>(qnext, qtail, n, P);
+  return cudaGetLastError();
+}
+
+}  // namespace nomad

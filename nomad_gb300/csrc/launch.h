@@ -1,0 +1,91 @@
+// launch.h -- host-side launch wrappers of the sm_103a kernels (kernels_*.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nomad {
+
+// Factor storage on the device: rows padded to `kpad` elements (a multiple of the
+// 16-byte vector: 4 fp32 or 8 bf16), padding kept at zero.
+struct DevFactors {
+  void* W = nullptr;  // [m * kpad]
+  void* H = nullptr;  // [n * kpad]
+  int32_t m = 0, n = 0, dim = 0, kpad = 0;
+  int32_t nvec = 0;       // kpad / elements-per-vector = lanes that hold a row
+  int32_t red_width = 0;  // power of two >= min(nvec, 32): shuffle-reduction width
+  int32_t bf16 = 0;       // storage: 0 fp32, 1 bf16
+};
+
+struct AsyncArgs {
+  DevFactors f;
+  const int2* ratings = nullptr;    // CSC-by-column {row, float bits}
+  const int4* segs = nullptr;       // {start lo, start hi, len, worker}
+  const int64_t* vl_ptr = nullptr;  // [n+1] visit list of each token
+  int32_t* tok_pos = nullptr;       // [n]
+  int32_t* tok_epoch = nullptr;     // [n]
+  const float* steps = nullptr;     // [n_steps] step size per pass count
+  int32_t n_steps = 0;
+  int32_t* qnext = nullptr;         // [n + P]
+  int32_t* qtail = nullptr;         // [P]
+  int32_t* ctrl = nullptr;          // [0] retired tokens, [1] device status
+  unsigned long long* progress = nullptr;  // [1] hop counter (batched)
+  unsigned long long* stats = nullptr;     // [0] updates [1] hops [2] empty polls
+  double* err_sum = nullptr;               // [1] online squared error
+  int32_t P = 0, n_active = 0, target_epoch = 0;
+  float lambda = 0.f;
+  uint32_t seed32 = 0;
+  int64_t budget_ns = 0;
+  int32_t exact = 0;
+  int32_t warps_per_block = 0, grid = 0;
+};
+
+struct ReplayArgs {
+  DevFactors f;
+  const int2* ratings = nullptr;
+  const int64_t* col_ptr = nullptr;
+  const float* steps = nullptr;
+  int32_t first_epoch = 0, n_epochs = 0;
+  float lambda = 0.f;
+  uint32_t seed32 = 0;
+  double* err_sum = nullptr;
+};
+
+struct DsgdArgs {
+  DevFactors f;
+  const int4* rates = nullptr;       // {row, col, float bits, 0} grouped by block
+  const int64_t* blk_ptr = nullptr;  // [innerB^2 + 1]
+  const int32_t* sched = nullptr;    // [innerB * innerB]: bj of row block bi in stratum i
+  int32_t innerB = 0;
+  float step = 0.f, lambda = 0.f;
+  int32_t iter = 0;
+  uint32_t seed32 = 0;
+  int32_t exact = 0;
+};
+
+struct SseArgs {
+  DevFactors f;
+  const int2* ratings = nullptr;
+  const int64_t* col_ptr = nullptr;
+  int64_t nnz = 0;
+  double* partials = nullptr;  // [grid] scratch
+  double* out = nullptr;       // [1]
+  int32_t grid = 0;
+};
+
+// Returns cudaError_t of the launch (cudaSuccess when nothing was launched).
+cudaError_t launch_async(const AsyncArgs& a, cudaStream_t s);
+cudaError_t async_occupancy(int bf16, int nv, int exact, int warps_per_block, int kpad,
+                            int* blocks_per_sm);
+cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);
+cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
+cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);
+cudaError_t launch_init_hash(const DevFactors& f, uint64_t seed, cudaStream_t s);
+cudaError_t launch_f32_to_store(const float* src, void* dst, int64_t rows, int32_t dim,
+                                int32_t kpad, int bf16, cudaStream_t s);
+cudaError_t launch_store_to_f32(const void* src, float* dst, int64_t rows, int32_t dim,
+                                int32_t kpad, int bf16, cudaStream_t s);
+cudaError_t launch_empty_queues(int32_t* qnext, int32_t* qtail, int32_t n, int32_t P,
+                                cudaStream_t s);
+
+}  // namespace nomad

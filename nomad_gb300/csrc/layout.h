@@ -1,0 +1,74 @@
+// layout.h -- host-side construction of the device data layout.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "common.h"
+
+namespace nomad {
+
+// One rating in CSC-by-column order: row index and the value's float bits.
+struct Rating {
+  int32_t row;
+  float val;
+};
+
+// Ratings grouped by column, rows ascending inside a column (what read_data builds
+// for one part, Code/nomad/nb_data.cpp:131-169).
+struct Csc {
+  int32_t m = 0, n = 0;
+  std::vector<int64_t> col_ptr;  // [n+1]
+  std::vector<Rating> ratings;   // [nnz]
+  int64_t nnz() const { return col_ptr.empty() ? 0 : col_ptr.back(); }
+};
+
+// A token visit: the ratings of one column owned by one worker.  16 bytes, read by
+// the device as an int4 {start lo, start hi, len, worker}.
+struct Segment {
+  int64_t start;
+  int32_t len;
+  int32_t worker;
+};
+static_assert(sizeof(Segment) == 16, "segment must be 16 bytes");
+
+struct AsyncLayout {
+  int32_t P = 0;
+  std::vector<int32_t> row_start;  // [P+1] first row of each worker's block
+  std::vector<int64_t> vl_ptr;     // [n+1] visit list of each column
+  std::vector<Segment> segs;       // visits, each column's list in its route order
+  std::vector<int32_t> qnext0;     // [n+P] initial queues (tokens in column order)
+  std::vector<int32_t> qtail0;     // [P]
+  int32_t n_active = 0;
+  int64_t max_column = 0;
+  int64_t max_segment = 0;
+};
+
+// DSGD blocks of one process (Code/competitor/sgd-mpi-omp.cpp:39-60, 539-588):
+// innerB x innerB blocks; entries of a block in reversed file order, so the device
+// walks forward through what sgd() walks backward.
+struct DsgdLayout {
+  int32_t innerB = 0, innerBm = 0, innerBn = 0;
+  std::vector<int64_t> blk_ptr;  // [innerB^2 + 1]
+  std::vector<int32_t> rates;    // 4 ints per entry: row, col, float bits, 0
+};
+
+// Build the CSC of a rating set given in the row-major file layout or as COO.
+// Fails on out-of-range indices and on repeated (row, column) cells.
+int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int threads);
+
+// Row blocks, visit lists (shuffled with `seed`) and the initial queues.
+int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
+                       AsyncLayout& out, int threads);
+
+int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
+                      DsgdLayout& out);
+
+// DSGD inner-stratum schedule of iteration `iter` (1-based): bj of row block bi in
+// stratum i at [i*innerB + bi] (sgd-mpi-omp.cpp:268-365 with B = 1).
+void dsgd_schedule(int32_t innerB, int32_t iter, int32_t strategy, std::vector<int32_t>& out);
+
+// Step size of pass `cnt` in float semantics (nomad_body.hpp:326-327).
+float step_size_f32(double lrate, double drate, int32_t cnt);
+
+}  // namespace nomad

@@ -1,0 +1,190 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle restates the reference's hot path on the CPU (see nomad_oracle.h for the
+reference lines each function follows).  Only tests/, __graft_entry__.smoke() and the
+cpu_baseline / reference leg of bench.py import this module; the product never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libnomad_oracle.so")
+_lib = None
+
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_u64 = ctypes.c_uint64
+_dbl = ctypes.c_double
+_ptr = ctypes.c_void_p
+
+
+def build():
+    """Compile the oracle with its Makefile (make is a no-op when up to date)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.oracle_step_f32.restype = ctypes.c_float
+        L.oracle_step_f32.argtypes = [_dbl, _dbl, _i32]
+        L.oracle_step_f64.restype = _dbl
+        L.oracle_step_f64.argtypes = [_dbl, _dbl, _i32]
+        L.oracle_mt19937_64_10000th.restype = _u64
+        L.oracle_init_factors.restype = None
+        L.oracle_init_factors.argtypes = [_i32, _i32, _i32, _u64, _i32, _ptr, _ptr]
+        for name in ("oracle_replay_f32", "oracle_replay_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _ptr, _i32, _i32,
+                          _dbl, _dbl, _dbl, _ptr]
+        for name in ("oracle_sse_f32", "oracle_sse_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _ptr, _ptr, _ptr]
+        for name in ("oracle_async_f32", "oracle_async_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _ptr, _i32, _i32,
+                          _dbl, _dbl, _dbl, _dbl, _u64, _ptr, _ptr, _ptr]
+        for name in ("oracle_dsgd_f32", "oracle_dsgd_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_i32, _i32, _i32, _i64, _ptr, _ptr, _ptr, _ptr, _ptr, _i32,
+                          _i32, _i32, _dbl, _dbl, _dbl, _i32]
+        L.oracle_dsgd_schedule.restype = ctypes.c_int
+        L.oracle_dsgd_schedule.argtypes = [_i32, _i32, _i32, _ptr]
+        L.oracle_row_major_to_csc.restype = ctypes.c_int
+        L.oracle_row_major_to_csc.argtypes = [_i32, _i32, _i64, _ptr, _ptr, _ptr, _ptr,
+                                              _ptr, _ptr]
+        L.oracle_read_header.restype = ctypes.c_int
+        L.oracle_read_header.argtypes = [ctypes.c_char_p, _ptr, _ptr, _ptr, _ptr]
+        L.oracle_read_matrix.restype = ctypes.c_int
+        L.oracle_read_matrix.argtypes = [ctypes.c_char_p, _ptr, _ptr, _ptr]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"{what} failed with status {rc}")
+
+
+def mt19937_64_10000th():
+    return int(lib().oracle_mt19937_64_10000th())
+
+
+def step(lrate, drate, cnt, dtype=np.float32):
+    if np.dtype(dtype) == np.float32:
+        return np.float32(lib().oracle_step_f32(lrate, drate, cnt))
+    return np.float64(lib().oracle_step_f64(lrate, drate, cnt))
+
+
+def init_factors(m, n, dim, seed, nthreads=1):
+    """Reference init (nb_main.cpp:450-455, :70-98) in double."""
+    W = np.empty((m, dim), np.float64)
+    H = np.empty((n, dim), np.float64)
+    lib().oracle_init_factors(m, n, dim, seed, nthreads, _p(W), _p(H))
+    return W, H
+
+
+def row_major_to_csc(m, n, row_counts, cols, vals):
+    row_counts = np.ascontiguousarray(row_counts, np.int32)
+    cols = np.ascontiguousarray(cols, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    nnz = cols.size
+    col_ptr = np.empty(n + 1, np.int64)
+    row_idx = np.empty(nnz, np.int32)
+    cv = np.empty(nnz, np.float64)
+    _check(lib().oracle_row_major_to_csc(m, n, nnz, _p(row_counts), _p(cols), _p(vals),
+                                         _p(col_ptr), _p(row_idx), _p(cv)),
+           "row_major_to_csc")
+    return col_ptr, row_idx, cv
+
+
+def replay(csc, W, H, first_epoch, n_epochs, lrate, drate, reg):
+    """In-place replay on W, H (float32 -> nomad_float, float64 -> nomad_double)."""
+    col_ptr, row_idx, vals = csc
+    m, dim = W.shape
+    n = H.shape[0]
+    assert W.flags.c_contiguous and H.flags.c_contiguous and W.dtype == H.dtype
+    err = np.zeros(max(n_epochs, 1), np.float64)
+    f = lib().oracle_replay_f32 if W.dtype == np.float32 else lib().oracle_replay_f64
+    _check(f(m, n, dim, _p(col_ptr), _p(row_idx), _p(vals), _p(W), _p(H), first_epoch,
+             n_epochs, lrate, drate, reg, _p(err)), "replay")
+    return err[:n_epochs]
+
+
+def sse(csc, W, H):
+    col_ptr, row_idx, vals = csc
+    m, dim = W.shape
+    n = H.shape[0]
+    s = np.zeros(1, np.float64)
+    c = np.zeros(1, np.int64)
+    f = lib().oracle_sse_f32 if W.dtype == np.float32 else lib().oracle_sse_f64
+    _check(f(m, n, dim, _p(col_ptr), _p(row_idx), _p(vals), _p(W), _p(H), _p(s), _p(c)),
+           "sse")
+    return float(s[0]), int(c[0])
+
+
+def rmse(csc, W, H):
+    s, c = sse(csc, W, H)
+    return float(np.sqrt(s / c)) if c else float("nan")
+
+
+def async_train(csc, W, H, nthreads, n_epochs=0, timeout_sec=0.0, lrate=0.001,
+                drate=0.1, reg=1.0, seed=12345):
+    col_ptr, row_idx, vals = csc
+    m, dim = W.shape
+    n = H.shape[0]
+    u = np.zeros(1, np.int64)
+    fl = np.zeros(1, np.int64)
+    t = np.zeros(1, np.float64)
+    f = lib().oracle_async_f32 if W.dtype == np.float32 else lib().oracle_async_f64
+    _check(f(m, n, dim, _p(col_ptr), _p(row_idx), _p(vals), _p(W), _p(H), nthreads,
+             n_epochs, timeout_sec, lrate, drate, reg, seed, _p(u), _p(fl), _p(t)),
+           "async")
+    return {"updates": int(u[0]), "failures": int(fl[0]), "seconds": float(t[0])}
+
+
+def dsgd(m, n, row_counts, cols, vals, W, H, nthreads, first_iter, n_iters, lrate,
+         decay, reg, stratum_strategy=0):
+    row_counts = np.ascontiguousarray(row_counts, np.int32)
+    cols = np.ascontiguousarray(cols, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    dim = W.shape[1]
+    f = lib().oracle_dsgd_f32 if W.dtype == np.float32 else lib().oracle_dsgd_f64
+    _check(f(m, n, dim, cols.size, _p(row_counts), _p(cols), _p(vals), _p(W), _p(H),
+             nthreads, first_iter, n_iters, lrate, decay, reg, stratum_strategy), "dsgd")
+
+
+def dsgd_schedule(innerB, it, stratum_strategy=0):
+    out = np.empty(innerB * innerB, np.int32)
+    _check(lib().oracle_dsgd_schedule(innerB, it, stratum_strategy, _p(out)),
+           "dsgd_schedule")
+    return out.reshape(innerB, innerB)
+
+
+def read_matrix(path):
+    fid = np.zeros(1, np.int32)
+    m = np.zeros(1, np.int32)
+    n = np.zeros(1, np.int32)
+    nnz = np.zeros(1, np.int64)
+    bpath = os.fsencode(path)
+    _check(lib().oracle_read_header(bpath, _p(fid), _p(m), _p(n), _p(nnz)), "read_header")
+    rc = np.empty(int(m[0]), np.int32)
+    cols = np.empty(int(nnz[0]), np.int32)
+    vals = np.empty(int(nnz[0]), np.float64)
+    _check(lib().oracle_read_matrix(bpath, _p(rc), _p(cols), _p(vals)), "read_matrix")
+    return {"file_id": int(fid[0]), "m": int(m[0]), "n": int(n[0]),
+            "row_counts": rc, "cols": cols, "vals": vals}

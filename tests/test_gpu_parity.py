@@ -1,0 +1,205 @@
+"""GPU parity against the CPU oracle, through the C-ABI.
+
+Bars (stated in each test):
+  * replay mode: GPU factors equal the oracle's nomad_float replay bit for bit (the
+    stated tolerance is 1e-5 relative per element; the kernel meets it with 0);
+  * async mode, exact arithmetic, one worker: bit-identical to replay (same schedule);
+  * async mode, many workers: per-epoch test RMSE within 0.5% of the FP64 oracle
+    (nomad_double replay) at equal epochs;
+  * DSGD, exact arithmetic: bit-identical to the oracle's DSGD restatement;
+  * evaluation: FP64-accumulated SSE within 1e-6 relative of the oracle's.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LR, DR, REG = 0.001, 0.1, 0.05
+
+
+def small_problem(ng, m=600, n=150, nnz_train=9000, nnz_test=1000, seed=12345):
+    return ng.synth(ng.synth_spec(1, m=m, n=n, nnz_train=nnz_train, nnz_test=nnz_test,
+                                  seed=seed))
+
+
+def relerr(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)))
+
+
+@pytest.mark.parametrize("dim", [32, 100])
+def test_replay_bit_exact(ng, O, gpu_ok, dim):
+    train, test = small_problem(ng)
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="replay") as nm:
+        nm.epoch(2)
+        nm.epoch(1)  # continues the pass count across calls
+        Wg, Hg = nm.factors()
+    Wo, Ho = W0.copy(), H0.copy()
+    O.replay(train.to_csc(), Wo, Ho, 0, 3, LR, DR, REG)
+    assert np.array_equal(Wg, Wo) and np.array_equal(Hg, Ho), (relerr(Wg, Wo), relerr(Hg, Ho))
+
+
+@pytest.mark.parametrize("dim", [1, 7, 33, 129, 200])
+def test_replay_odd_dims(ng, O, gpu_ok, dim):
+    """Row padding (dim not a multiple of 4) and 2 / 4 vectors per lane."""
+    train, test = small_problem(ng, m=300, n=80, nnz_train=3000, nnz_test=300)
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 7, 3)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="replay") as nm:
+        nm.epoch(2)
+        Wg, Hg = nm.factors()
+    Wo, Ho = W0.copy(), H0.copy()
+    O.replay(train.to_csc(), Wo, Ho, 0, 2, LR, DR, REG)
+    assert np.array_equal(Wg, Wo) and np.array_equal(Hg, Ho), (relerr(Wg, Wo), relerr(Hg, Ho))
+
+
+def test_replay_workload1_per_element(ng, O, gpu_ok):
+    """The 10,000 x 2,000 workload, k = 100: per-element relative error <= 1e-5."""
+    train, test = ng.synth(1)
+    dim = 100
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="replay") as nm:
+        nm.epoch(2)
+        Wg, Hg = nm.factors()
+    Wo, Ho = W0.copy(), H0.copy()
+    O.replay(train.to_csc(), Wo, Ho, 0, 2, LR, DR, REG)
+    assert relerr(Wg, Wo) <= 1e-5 and relerr(Hg, Ho) <= 1e-5
+
+
+def test_async_one_worker_exact_equals_replay(ng, O, gpu_ok):
+    """One worker: the queue is FIFO in column order, so async == replay exactly."""
+    train, test = small_problem(ng)
+    dim = 32
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="async", workers=1, exact=1) as nm:
+        st = nm.epoch(3)
+        Wg, Hg = nm.factors()
+    assert st["updates"] == 3 * train.nnz
+    Wo, Ho = W0.copy(), H0.copy()
+    O.replay(train.to_csc(), Wo, Ho, 0, 3, LR, DR, REG)
+    assert np.array_equal(Wg, Wo) and np.array_equal(Hg, Ho), (relerr(Wg, Wo), relerr(Hg, Ho))
+
+
+@pytest.mark.parametrize("workers", [0, 7, 64])
+def test_async_counts(ng, gpu_ok, workers):
+    """Every rating is visited once per epoch (u=); one hop per (worker, column) visit."""
+    train, test = small_problem(ng)
+    with ng.Nomad(train, test, dim=32, lrate=LR, drate=DR, reg=REG, mode="async",
+                  workers=workers) as nm:
+        info = nm.info()
+        st = nm.epoch(2)
+        st2 = nm.epoch(1)
+    assert st["updates"] == 2 * train.nnz
+    assert st["hops"] == 2 * info["segments"]
+    assert st2["updates"] == train.nnz and st2["epochs_done"] == 3
+    if workers:
+        assert info["workers"] == workers
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_async_rmse_vs_fp64_oracle(ng, O, gpu_ok, precision):
+    """10,000 x 2,000 workload, 20 epochs: test RMSE within 0.5% of the FP64 oracle
+    (nomad_double replay) at every epoch."""
+    train, test = ng.synth(1)
+    dim, epochs = 100, 20
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    gpu = []
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="async", precision=precision) as nm:
+        for _ in range(epochs):
+            nm.epoch(1)
+            gpu.append(nm.rmse()[1])
+    csc, tcsc = train.to_csc(), test.to_csc()
+    Wd, Hd = W0.astype(np.float64), H0.astype(np.float64)
+    ref = []
+    for e in range(epochs):
+        O.replay(csc, Wd, Hd, e, 1, LR, DR, REG)
+        ref.append(O.rmse(tcsc, Wd, Hd))
+    gap = np.abs(np.array(gpu) - np.array(ref)) / np.array(ref)
+    assert gap.max() <= 0.005, (gap.max(), gpu[-1], ref[-1])
+
+
+def test_sse_kernel_vs_oracle(ng, O, gpu_ok):
+    train, test = small_problem(ng, m=2000, n=500, nnz_train=60000, nnz_test=6000)
+    dim = 100
+    rng = np.random.default_rng(3)
+    W = rng.standard_normal((train.m, dim)).astype(np.float32) * 0.1
+    H = rng.standard_normal((train.n, dim)).astype(np.float32) * 0.1
+    with ng.Nomad(train, test, W0=W, H0=H, dim=dim, mode="async") as nm:
+        s_tr, c_tr, s_te, c_te = nm.sse()
+    o_tr, oc_tr = O.sse(train.to_csc(), W.astype(np.float64), H.astype(np.float64))
+    o_te, oc_te = O.sse(test.to_csc(), W.astype(np.float64), H.astype(np.float64))
+    assert (c_tr, c_te) == (oc_tr, oc_te) == (train.nnz, test.nnz)
+    assert abs(s_tr - o_tr) <= 1e-6 * o_tr and abs(s_te - o_te) <= 1e-6 * o_te
+
+
+@pytest.mark.parametrize("strategy", [0, 2])
+def test_dsgd_exact_vs_oracle(ng, O, gpu_ok, strategy):
+    train, test = small_problem(ng, m=500, n=120, nnz_train=8000, nnz_test=500)
+    dim, nthreads = 40, 3
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 5, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=0.01, drate=0.1, reg=REG,
+                  mode="dsgd", exact=1, dsgd_inner_blocks=2 * nthreads,
+                  dsgd_strategy=strategy) as nm:
+        st = nm.epoch(3)
+        Wg, Hg = nm.factors()
+    assert st["updates"] == 3 * train.nnz
+    Wo, Ho = W0.copy(), H0.copy()
+    O.dsgd(train.m, train.n, train.row_counts, train.cols, train.vals, Wo, Ho, nthreads, 1, 3,
+           0.01, 0.1, REG, strategy)
+    assert np.array_equal(Wg, Wo) and np.array_equal(Hg, Ho), (relerr(Wg, Wo), relerr(Hg, Ho))
+
+
+def test_dsgd_fast_rmse(ng, O, gpu_ok):
+    train, test = ng.synth(1)
+    dim = 100
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="dsgd", dsgd_inner_blocks=64) as nm:
+        nm.epoch(5)
+        rm = nm.rmse()[1]
+    Wo, Ho = W0.astype(np.float64), H0.astype(np.float64)
+    O.dsgd(train.m, train.n, train.row_counts, train.cols, train.vals, Wo, Ho, 32, 1, 5,
+           LR, DR, REG, 0)
+    ref = O.rmse(test.to_csc(), Wo, Ho)
+    assert abs(rm - ref) <= 0.005 * ref, (rm, ref)
+
+
+def test_timeout_is_a_status_and_context_survives(ng, gpu_ok):
+    """A device wait that can never be satisfied (no token is ever enqueued) ends in
+    NOMAD_ERR_TIMEOUT after the spin budget instead of hanging; the context stays
+    usable, and a context without the hook trains normally."""
+    train, test = small_problem(ng)
+    p = ng.default_params(dim=32, lrate=LR, drate=DR, reg=REG, mode="async",
+                          spin_budget_ms=200, debug_flags=1)
+    with ng.Nomad(train, test, params=p) as nm:
+        for _ in range(2):
+            with pytest.raises(ng.NomadError) as ei:
+                nm.epoch(1)
+            assert ei.value.status == -4
+        assert nm.epoch(0)["epochs_done"] == 0
+        assert np.isfinite(nm.rmse()[0])
+    p.debug_flags = 0
+    with ng.Nomad(train, test, params=p) as nm2:
+        st = nm2.epoch(1)
+        assert st["updates"] == train.nnz
+
+
+def test_factor_roundtrip(ng, gpu_ok):
+    train, test = small_problem(ng)
+    rng = np.random.default_rng(0)
+    W = rng.standard_normal((train.m, 30)).astype(np.float32)
+    H = rng.standard_normal((train.n, 30)).astype(np.float32)
+    with ng.Nomad(train, test, dim=30, mode="async") as nm:
+        nm.set_factors(W, H)
+        W2, H2 = nm.factors()
+    assert np.array_equal(W, W2) and np.array_equal(H, H2)
+    with ng.Nomad(train, test, dim=30, mode="async", precision="bf16") as nm:
+        nm.set_factors(W, H)
+        W3, _ = nm.factors()
+    assert np.max(np.abs(W3 - W) / np.maximum(np.abs(W), 1e-6)) <= 2 ** -8

@@ -1,0 +1,371 @@
+#!/usr/bin/env python3
+"""Benchmark of the asynchronous NOMAD SGD hot path on one GB300.
+
+Workload: the 480,189 x 17,770 rating matrix with 100,480,507 training and 1,408,395
+test ratings (user degrees Zipf(0.8), item degrees Zipf(1.1), integer ratings 1-5 from a
+planted rank-20 model), k = 100, lrate 0.002, drate 0.05, reg 0.05: seeded synthetic
+data with the shape of the Netflix-prize matrix (the dataset itself is not used).
+
+One step = one epoch of the async NOMAD kernel: every training rating updated once,
+column tokens passed between 4,864 worker warps through device queues.  Both storage
+forms run (fp32 and bf16 with stochastic rounding); the headline value is the bf16
+form.  The device-resident number (`value`) sums CUDA-event time of the K timed epoch
+launches; `e2e` times the whole job through the C-ABI from host buffers (init with the
+H2D copy of the ratings, K epochs, an RMSE read-back per epoch, the factor read-back).
+Test RMSE is evaluated after every epoch, outside the timed launches, as the reference
+excludes testing time from training time (Code/nomad/nb_main.cpp:265-266).
+
+`--impl reference` times the CPU restatement of the reference's updater loop (the
+oracle's asynchronous float mode, every host core) on the same workload: the reference
+itself needs MPI, TBB, Boost and glog, none of which exist on these machines.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rating updates/s & time-to-test-RMSE on 1 GB300, BF16 vs plain FP32 GPU form"
+UNIT = "rating updates/s"
+WORKLOAD_ID = 2
+HP = dict(dim=100, lrate=0.002, drate=0.05, reg=0.05)
+BYTES_PER_UPDATE = {"fp32": 2 * 100 * 4 + 8, "bf16": 2 * 100 * 2 + 8}  # w_i read+write, index, value
+TARGET_FILE = os.path.join(ROOT, "tests", "golden", "workload2_fp64_rmse.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "async_kernel_traffic.json")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="wall-clock sample of the CPU baseline")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workers", type=int, default=0)
+    ap.add_argument("--wpb", type=int, default=0)
+    ap.add_argument("--bps", type=int, default=0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------
+class Dist:
+    """torchrun plumbing: replicas only (one independent problem per GPU)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group(backend="gloo")
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, value, op):
+        if not self.pg:
+            return value
+        import torch
+        t = torch.tensor([float(value)], dtype=torch.float64)
+        self.pg.all_reduce(t, op={"max": self.pg.ReduceOp.MAX, "sum": self.pg.ReduceOp.SUM}[op])
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling while the timed launches run."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(device)], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        self.active = False
+        self.marks = []
+
+    def mark(self, on):
+        self.marks.append((time.time(), on))
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(", ") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            if len(r) >= 9:
+                for nm_, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm_)
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def target_curve():
+    try:
+        with open(TARGET_FILE) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+# ---------------------------------------------------------------------------------
+def run_form(ng, train, test, precision, W, K, device, args, clocks=None):
+    """Fresh context; W warm-up + K timed epochs, test RMSE after every epoch."""
+    kw = dict(HP, precision=precision, mode="async", device=device, init_parts=16,
+              workers=args.workers, warps_per_block=args.wpb, blocks_per_sm=args.bps)
+    t0 = time.perf_counter()
+    nm = ng.Nomad(train, test, **kw)
+    init_s = time.perf_counter() - t0
+    info = nm.info()
+    epochs = []
+    for e in range(W + K):
+        timed = e >= W
+        if timed and clocks:
+            clocks.mark(True)
+        st = nm.epoch(1)
+        if timed and clocks:
+            clocks.mark(False)
+        tr, te = nm.rmse()
+        epochs.append({"device_ms": st["device_ms"], "host_s": st["host_seconds"],
+                       "updates": st["updates"], "hops": st["hops"],
+                       "failures": st["failures"], "train_rmse": tr, "test_rmse": te})
+    nm.close()
+    timed = epochs[W:]
+    dev_s = sum(x["device_ms"] for x in timed) / 1e3
+    upd = sum(x["updates"] for x in timed)
+    return {"precision": precision, "init_s": init_s, "info": info, "epochs": epochs,
+            "timed_device_s": dev_s, "timed_updates": upd,
+            "updates_per_s": upd / dev_s if dev_s > 0 else 0.0,
+            "ms_per_step": 1e3 * dev_s / max(K, 1),
+            "host_updates_per_s": upd / max(sum(x["host_s"] for x in timed), 1e-12)}
+
+
+def time_to_target(res, curve):
+    """Training seconds (device) until test RMSE <= 1.005 x the FP64 oracle's RMSE at the
+    last epoch run, and the largest per-epoch gap to the oracle at equal epochs."""
+    if not curve:
+        return None
+    ref = curve["test_rmse"]
+    E = min(len(res["epochs"]), len(ref))
+    target = ref[E - 1] * 1.005
+    t, hit = 0.0, None
+    for e in range(E):
+        t += res["epochs"][e]["device_ms"] / 1e3
+        if hit is None and res["epochs"][e]["test_rmse"] <= target:
+            hit = t
+    gaps = [abs(res["epochs"][e]["test_rmse"] - ref[e]) / ref[e] for e in range(E)]
+    return {"seconds": hit, "target_rmse": target, "oracle_epochs": E,
+            "final_gap": gaps[-1], "max_gap": max(gaps)}
+
+
+def e2e_run(ng, train, test, K, device, args):
+    """The whole job through the C-ABI from host buffers."""
+    kw = dict(HP, precision="bf16", mode="async", device=device, init_parts=16,
+              workers=args.workers, warps_per_block=args.wpb, blocks_per_sm=args.bps)
+    t0 = time.perf_counter()
+    nm = ng.Nomad(train, test, **kw)
+    upd = 0
+    for _ in range(K):
+        upd += nm.epoch(1)["updates"]
+        nm.rmse()
+    nm.factors()
+    info = nm.info()
+    nm.close()
+    dt = time.perf_counter() - t0
+    return {"value": upd / dt, "unit": UNIT,
+            "h2d_bytes_per_step": int(info["h2d_bytes"] // max(K, 1)),
+            "d2h_bytes_per_step": int(info["d2h_bytes"] // max(K, 1)),
+            "seconds": dt}
+
+
+def cpu_baseline(train, seconds):
+    """The oracle's asynchronous float mode (the reference's updater loop restated),
+    every host core, one wall-clock interval of the same workload."""
+    import nomad_gb300 as ng
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    csc = O.row_major_to_csc(train.m, train.n, train.row_counts, train.cols, train.vals)
+    W, H = ng.reference_init(train.m, train.n, HP["dim"], 12345, cores)
+    st = O.async_train(csc, W, H, nthreads=cores, n_epochs=0, timeout_sec=seconds,
+                       lrate=HP["lrate"], drate=HP["drate"], reg=HP["reg"], seed=12345)
+    return {"value": st["updates"] / st["seconds"], "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": (f"480,189x17,770 / 100.5M-rating workload, CPU restatement of the "
+                       f"reference updater (float), {cores} threads, one {seconds:.0f} s "
+                       f"training interval from the reference init ({st['updates']} updates)")}
+
+
+def config_block(K, W):
+    return {"workload": "480,189 x 17,770, 100,480,507 train / 1,408,395 test ratings "
+                        "(Zipf(0.8) users, Zipf(1.1) items, planted rank 20, ratings 1-5)",
+            "dim": HP["dim"], "lrate": HP["lrate"], "drate": HP["drate"], "reg": HP["reg"],
+            "step": "one epoch (every training rating updated once)",
+            "mode": "async NOMAD, one worker per warp",
+            "l2": "inputs larger than L2 (800 MB ratings + 96-192 MB factors per epoch)",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------------
+def main_reference(args, dist):
+    if dist.rank != 0:
+        return
+    import nomad_gb300 as ng
+    from oracle import oracle as O
+    train, test = ng.synth(WORKLOAD_ID)
+    cores = os.cpu_count() or 1
+    csc = O.row_major_to_csc(train.m, train.n, train.row_counts, train.cols, train.vals)
+    W, H = ng.reference_init(train.m, train.n, HP["dim"], 12345, cores)
+    sample_s = max(1.0, min(10.0, 150.0 / max(args.steps + args.warmup, 1)))
+    for _ in range(args.warmup):
+        O.async_train(csc, W, H, nthreads=cores, timeout_sec=sample_s, lrate=HP["lrate"],
+                      drate=HP["drate"], reg=HP["reg"])
+    upd, secs = 0, 0.0
+    for _ in range(args.steps):
+        st = O.async_train(csc, W, H, nthreads=cores, timeout_sec=sample_s, lrate=HP["lrate"],
+                           drate=HP["drate"], reg=HP["reg"])
+        upd += st["updates"]
+        secs += st["seconds"]
+    v = upd / secs
+    sample = (f"{args.steps} training intervals of {sample_s:.1f} s each on the 480,189x17,770 "
+              f"workload, {cores} threads, CPU restatement of the reference updater (float)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_block(args.steps, args.warmup),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (MPI+TBB+Boost+glog) cannot be built on these hosts; this is "
+                "the oracle's restatement of its updater loop"}), flush=True)
+
+
+def main_ours(args, dist):
+    import nomad_gb300 as ng
+    device = dist.local
+    if not ng.device_ok(device):
+        raise SystemExit(f"cuda:{device} is not an sm_103 device")
+    K, W = args.steps, args.warmup
+    t = time.perf_counter()
+    train, test = ng.synth(WORKLOAD_ID)
+    log(f"[bench] workload generated in {time.perf_counter() - t:.1f} s "
+        f"(nnz {train.nnz} / {test.nnz})")
+    clocks = Clocks(device)
+    dist.barrier()
+    res = {}
+    for form in ("fp32", "bf16"):
+        res[form] = run_form(ng, train, test, form, W, K, device, args,
+                             clocks if form == "bf16" else None)
+        log(f"[bench] {form}: {res[form]['updates_per_s']:.4g} updates/s, "
+            f"{res[form]['ms_per_step']:.2f} ms/epoch, test RMSE "
+            f"{res[form]['epochs'][-1]['test_rmse']:.5f}, init {res[form]['init_s']:.1f} s")
+    clk = clocks.stop()
+    dist.barrier()
+    b = res["bf16"]
+    # whole-job aggregate over ranks: updates summed, time = slowest rank
+    tot_upd = dist.reduce(b["timed_updates"], "sum")
+    max_s = dist.reduce(b["timed_device_s"], "max")
+    value = tot_upd / max_s
+    e2e = None if args.no_e2e else e2e_run(ng, train, test, K, device, args)
+    if e2e and dist.world > 1:
+        e2e["value"] = dist.reduce(e2e["value"], "sum")
+    peak, peak_kind = hbm_peak()
+    achieved = BYTES_PER_UPDATE["bf16"] * b["timed_updates"] / b["timed_device_s"] / 1e9
+    traffic = None
+    try:
+        with open(TRAFFIC_FILE) as f:
+            tr = json.load(f)
+        traffic = tr["dram_bytes_per_update"]["bf16"] * b["timed_updates"] / max(K, 1)
+    except (OSError, KeyError, ValueError):
+        pass
+    curve = target_curve()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": K, "warmup": W, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "compute_dtype": "f32 (bf16 storage, stochastic-rounding write-back)",
+        "data": "synthetic (seeded, shape of the 480,189x17,770 Netflix-prize matrix)",
+        "config": config_block(K, W),
+        "fp32": {"value": res["fp32"]["updates_per_s"], "ms_per_step": res["fp32"]["ms_per_step"],
+                 "roofline_frac": BYTES_PER_UPDATE["fp32"] * res["fp32"]["updates_per_s"] / 1e9 / peak,
+                 "final_test_rmse": res["fp32"]["epochs"][-1]["test_rmse"]},
+        "bf16_over_fp32": b["updates_per_s"] / res["fp32"]["updates_per_s"],
+        "final_test_rmse": b["epochs"][-1]["test_rmse"],
+        "time_to_target": {"bf16": time_to_target(b, curve),
+                           "fp32": time_to_target(res["fp32"], curve)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"of {peak_kind}",
+                     "bytes_per_update": BYTES_PER_UPDATE["bf16"],
+                     "kernel": "nomad_async_kernel<bf16> (one launch per epoch)"},
+        "clocks": clk,
+        "e2e": e2e,
+        "gpu_launches": K,
+        "workers": b["info"]["workers"], "segments_per_epoch": b["info"]["segments"],
+        "max_column": b["info"]["max_column"],
+        "host_updates_per_s": b["host_updates_per_s"],
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(train, args.cpu_seconds)
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            main_reference(args, dist)
+        else:
+            main_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

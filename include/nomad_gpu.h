@@ -128,6 +128,8 @@ typedef struct nomad_gpu_info {
   int32_t grid_blocks, block_threads, num_sms, inner_blocks;
   int64_t device_bytes;     /* device memory held by the context                   */
   int32_t mode, precision;
+  int64_t h2d_bytes;        /* host-to-device bytes copied since init (cumulative) */
+  int64_t d2h_bytes;        /* device-to-host bytes copied since init (cumulative) */
 } nomad_gpu_info;
 
 typedef struct nomad_gpu_ctx nomad_gpu_ctx; /* opaque */

@@ -55,6 +55,7 @@ struct nomad_gpu_ctx {
   double* sse_out = nullptr;
   int32_t sse_grid = 0;
   int32_t epochs_done = 0;
+  int64_t h2d_bytes = 0, d2h_bytes = 0;
 };
 
 namespace {
@@ -92,6 +93,7 @@ int upload(nomad_gpu_ctx* c, T** p, const T* src, size_t count) {
   int rc = dalloc(c, p, count);
   if (rc) return rc;
   if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  c->h2d_bytes += static_cast<int64_t>(count * sizeof(T));
   return NOMAD_OK;
 }
 
@@ -111,6 +113,7 @@ int ensure_steps(nomad_gpu_ctx* c, int32_t needed) {
   RC(dalloc(c, &d, cap));
   CK(cudaMemcpyAsync(d, h.data(), cap * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  c->h2d_bytes += static_cast<int64_t>(cap * sizeof(float));
   c->steps = d;  // the previous table stays allocated until destroy (small)
   c->n_steps = cap;
   return NOMAD_OK;
@@ -134,6 +137,7 @@ int put_factor(nomad_gpu_ctx* c, void* dst, const float* src, int64_t rows) {
                                      f.kpad, f.bf16, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) rc = cuda_fail(e, "factor upload");
+    c->h2d_bytes += nr * f.dim * static_cast<int64_t>(sizeof(float));
   }
   cudaFree(stage);
   return rc;
@@ -155,6 +159,7 @@ int get_factor(nomad_gpu_ctx* c, const void* src, float* dst, int64_t rows) {
                           cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) rc = cuda_fail(e, "factor download");
+    c->d2h_bytes += nr * f.dim * static_cast<int64_t>(sizeof(float));
   }
   cudaFree(stage);
   return rc;
@@ -335,6 +340,7 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   CK(cudaMemcpy(ctrl, c->ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(stats, c->stats, sizeof(stats), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(&esum, c->err_sum, sizeof(double), cudaMemcpyDeviceToHost));
+  c->d2h_bytes += static_cast<int64_t>(sizeof(ctrl) + sizeof(stats) + sizeof(double));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   if (st) {
@@ -517,6 +523,7 @@ int nomad_gpu_sse(nomad_gpu_ctx* c, double* train_sse, int64_t* train_count, dou
   double h[2];
   CK(cudaMemcpyAsync(h, c->sse_out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  c->d2h_bytes += static_cast<int64_t>(sizeof(h));
   if (train_sse) *train_sse = h[0];
   if (test_sse) *test_sse = h[1];
   if (train_count) *train_count = c->nnz_train;
@@ -572,6 +579,8 @@ int nomad_gpu_get_info(nomad_gpu_ctx* c, nomad_gpu_info* info) {
   info->device_bytes = c->device_bytes;
   info->mode = c->prm.mode;
   info->precision = c->prm.precision;
+  info->h2d_bytes = c->h2d_bytes;
+  info->d2h_bytes = c->d2h_bytes;
   return NOMAD_OK;
 }
 

@@ -1,0 +1,77 @@
+"""The nomad_gpu driver: the reference's command-line surface (nomad_option.cpp:16-77,
+plus --path) and its statistics block (nb_main.cpp:267-285)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "nomad_gb300", "_build", "nomad_gpu")
+
+
+def run(*args, timeout=300):
+    return subprocess.run([CLI, *args], capture_output=True, text=True, timeout=timeout)
+
+
+def test_help_and_usage(ng):
+    r = run("--help")
+    assert r.returncode == 1
+    for flag in ("--lrate", "--drate", "--reg", "--seed", "--dim", "--timeout", "--input",
+                 "--path", "--output", "--nthreads"):
+        assert flag in r.stderr
+
+
+def test_missing_path_is_rejected(ng):
+    r = run("--lrate", "0.01")
+    assert r.returncode == 1 and "input path has to be specified." in r.stderr
+
+
+def test_bad_value_and_unknown_option(ng):
+    assert run("--path", "x", "--lrate", "abc").returncode == 1
+    assert run("--path", "x", "--bogus", "1").returncode == 1
+    r = run("--path", "x", "--cptype", "weird")
+    assert r.returncode == 1 and "checkpoint type is inalid." in r.stderr
+
+
+def test_unreadable_data_exits_11(ng, tmp_path):
+    r = run("--path", str(tmp_path))
+    assert r.returncode == 11 and "error in reading training file" in r.stderr
+
+
+def _write_dataset(ng, d):
+    tr, te = ng.synth(ng.synth_spec(1, m=400, n=120, nnz_train=6000, nnz_test=600))
+    tr.write(os.path.join(d, "train.dat"))
+    te.write(os.path.join(d, "test.dat"))
+    return tr, te
+
+
+@pytest.mark.gpu
+def test_end_to_end_run(ng, gpu_ok, tmp_path):
+    tr, te = _write_dataset(ng, str(tmp_path))
+    out = str(tmp_path / "factors")
+    r = run("--path", str(tmp_path), "--dim", "16", "--lrate", "0.01", "--reg", "0.05",
+            "--timeout", "0.2", "0.4", "--pause", "0", "--nthreads", "2", "--output", out)
+    assert r.returncode == 0, r.stderr
+    blocks = re.findall(r"current test RMSE: ([0-9.]+)", r.stdout)
+    assert len(blocks) == 2
+    m = re.findall(r"detail: train: s=([0-9.]+), c=(\d+); test: s=([0-9.]+), c=(\d+); "
+                   r"u=(\d+), f=(\d+), s=(\d+)", r.stdout)
+    assert len(m) == 2 and int(m[0][1]) == tr.nnz and int(m[0][3]) == te.nnz
+    assert int(m[1][4]) % tr.nnz == 0 and int(m[1][4]) > 0
+    lines = open(out + "0").read().splitlines()
+    assert len(lines) == tr.m + tr.n
+    assert lines[0].startswith("row,0,") and lines[-1].startswith(f"column,{tr.n - 1},")
+    assert len(lines[0].split(",")) == 2 + 16
+
+
+@pytest.mark.gpu
+def test_epochs_and_modes(ng, gpu_ok, tmp_path):
+    _write_dataset(ng, str(tmp_path))
+    for mode in ("async", "replay", "dsgd"):
+        r = run("--path", str(tmp_path), "--dim", "8", "--epochs", "2", "--pause", "0",
+                "--mode", mode, "--reg", "0.05", "--lrate", "0.01")
+        assert r.returncode == 0, (mode, r.stderr)
+        rm = float(re.findall(r"current test RMSE: ([0-9.]+)", r.stdout)[0])
+        assert np.isfinite(rm)

@@ -179,6 +179,36 @@ const char* nomad_gpu_last_error(void);
 /* 1 when a usable sm_103 device is present, else 0. */
 int nomad_gpu_device_ok(int32_t device);
 
+/* ---- evaluation without device allocation ---------------------------------------
+ * No counterpart in the reference: it is an extra entry point for callers that
+ * cannot obtain device memory from the CUDA allocator -- a host runtime that hands
+ * out device memory only from its own pool, or a latency-sensitive loop that must
+ * not call cudaMalloc/cudaFree because cudaFree waits for the whole device.  Such a
+ * caller owns every buffer (inputs and the output) and this call allocates nothing:
+ * the evaluation kernel's per-block FP64 partial sums live in one fixed array
+ * compiled into the library (NOMAD_NOALLOC_MAX_BLOCKS doubles, 16 KiB on every GPU
+ * that loads the library, held until the process exits).
+ *
+ * Computes, asynchronously on `stream` (a cudaStream_t, NULL = default stream), the
+ * squared-error sum  sum (<h_j, w_i> - v)^2  of one CSC rating set and writes it to
+ * the device double *sse_out.  Layout (as nomad_gpu_init builds it):
+ *   W        [m x kpad] factor rows, H [n x kpad] factor columns, row-major, in fp32
+ *            (precision NOMAD_PREC_FP32, kpad = dim rounded up to 4) or bf16
+ *            (NOMAD_PREC_BF16_SR, kpad = dim rounded up to 8); padding zero;
+ *   ratings  nnz pairs {int32 row, float value}, grouped by column;
+ *   col_ptr  n + 1 int64 offsets of the columns in `ratings`.
+ * blocks = 0 picks 8 per SM (at most NOMAD_NOALLOC_MAX_BLOCKS); larger values are
+ * rejected with NOMAD_ERR_INVALID_ARG.  The first call on a device looks up the
+ * array's device address with that device made current (it is restored afterwards);
+ * make that first call before capturing any stream.  Every call uses the same array,
+ * so calls that overlap on the GPU (different streams, no ordering) race and give
+ * wrong sums; each call rewrites every partial it reads, so nothing needs clearing. */
+#define NOMAD_NOALLOC_MAX_BLOCKS 2048
+int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t n, int32_t dim,
+                          const void* W, const void* H, const void* ratings,
+                          const int64_t* col_ptr, int64_t nnz, int32_t blocks,
+                          double* sse_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,7 @@ INIT_REFERENCE, INIT_HASH = 0, 1
 FILE_ID_INT, FILE_ID_LONG = 1211216, 1015
 SYNTH_UNIFORM, SYNTH_DEGREES = 0, 1
 LAW_UNIFORM, LAW_ZIPF, LAW_GEOMETRIC = 0, 1, 2
+NOALLOC_MAX_BLOCKS = 2048
 
 
 class Params(ctypes.Structure):
@@ -101,6 +102,8 @@ SIGNATURES = {
     "nomad_gpu_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "nomad_gpu_last_error": (ctypes.c_char_p, []),
     "nomad_gpu_device_ok": (ctypes.c_int, [c_i32]),
+    "nomad_gpu_sse_noalloc": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,
+                                             c_i64, c_i32, c_vp, c_vp]),
     "nomad_io_read_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_i32),
                                             ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
                                             ctypes.POINTER(c_i64)]),

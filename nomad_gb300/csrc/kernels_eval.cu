@@ -2,6 +2,9 @@
 // initialisation and layout-conversion kernels for sm_103a.
 #include <cuda_bf16.h>
 
+#include <mutex>
+
+#include "common.h"
 #include "device_common.cuh"
 #include "launch.h"
 
@@ -246,3 +249,94 @@ cudaError_t launch_empty_queues(int32_t* qnext, int32_t* qtail, int32_t n, int32
 }
 
 }  // namespace nomad
+
+// ---------------------------------------------------------------------------------
+// nomad_gpu_sse_noalloc: the evaluation kernel with its partial sums in a fixed array
+// compiled into this file, for callers that cannot allocate device memory.
+// ---------------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) double g_noalloc_partials[NOMAD_NOALLOC_MAX_BLOCKS];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t n,
+                                     int32_t dim, const void* W, const void* H,
+                                     const void* ratings, const int64_t* col_ptr,
+                                     int64_t nnz, int32_t blocks, double* sse_out,
+                                     void* stream) {
+  nomad::clear_last_error();
+  if (device < 0 || device >= kMaxDevices)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "device %d out of range", device);
+  if (precision != NOMAD_PREC_FP32 && precision != NOMAD_PREC_BF16_SR)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (n < 0 || dim <= 0 || nnz < 0 || !sse_out || (nnz > 0 && (!W || !H || !ratings || !col_ptr)))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid sizes or null pointers");
+  if (blocks < 0 || blocks > NOMAD_NOALLOC_MAX_BLOCKS)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG,
+               "blocks = %d exceeds the fixed partial-sum array of %d blocks", blocks,
+               NOMAD_NOALLOC_MAX_BLOCKS);
+  const int bf16 = precision == NOMAD_PREC_BF16_SR;
+  const int E = bf16 ? 8 : 4;
+  nomad::DevFactors f;
+  f.W = const_cast<void*>(W);
+  f.H = const_cast<void*>(H);
+  f.n = n;
+  f.dim = dim;
+  f.kpad = (dim + E - 1) / E * E;
+  f.nvec = f.kpad / E;
+  f.bf16 = bf16;
+  f.red_width = 32;
+  if (f.nvec > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "dim %d exceeds the supported maximum", dim);
+  int prev = -1;
+  cudaError_t e = cudaGetDevice(&prev);
+  if (e != cudaSuccess) NOMAD_FAIL(NOMAD_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess)
+    NOMAD_FAIL(NOMAD_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+  int rc = NOMAD_OK;
+  double* scratch = nullptr;
+  {
+    // once per device, with that device current: the device address of the array
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (e == cudaSuccess) g_noalloc_addr[device] = static_cast<double*>(p);
+    }
+    scratch = g_noalloc_addr[device];
+  }
+  if (!scratch) {
+    nomad::set_last_error("cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    rc = NOMAD_ERR_CUDA;
+  } else {
+    int sms = 0;
+    if (blocks == 0) {
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+      blocks = e == cudaSuccess ? std::min(8 * sms, NOMAD_NOALLOC_MAX_BLOCKS) : 0;
+    }
+    if (blocks <= 0) {
+      nomad::set_last_error("cudaDeviceGetAttribute: %s", cudaGetErrorString(e));
+      rc = NOMAD_ERR_CUDA;
+    } else {
+      nomad::SseArgs a;
+      a.f = f;
+      a.ratings = static_cast<const int2*>(ratings);
+      a.col_ptr = col_ptr;
+      a.nnz = nnz;
+      a.partials = scratch;
+      a.out = sse_out;
+      a.grid = blocks;
+      e = nomad::launch_sse(a, static_cast<cudaStream_t>(stream));
+      if (e != cudaSuccess) {
+        nomad::set_last_error("evaluation launch: %s", cudaGetErrorString(e));
+        rc = NOMAD_ERR_CUDA;
+      }
+    }
+  }
+  if (prev != device) cudaSetDevice(prev);
+  return rc;
+}

@@ -83,7 +83,12 @@ typedef struct nomad_gpu_params {
   int32_t spin_budget_ms; /* device waits give up after this long without global
                              progress and the call returns NOMAD_ERR_TIMEOUT (2000)  */
   int32_t debug_flags; /* test hooks; bit 0 = enqueue no tokens (forces a timeout)   */
-  int32_t reserved[8];
+  int32_t long_visit;  /* ASYNC: visits with at least this many ratings run the blocked
+                          (7-rating) path with TMA-staged rows; 0 = default 14        */
+  int32_t priority_permille; /* ASYNC: columns with at least this many permille of the
+                          largest column's ratings use the workers' priority queues;
+                          0 = default 50, negative = no priority queue                */
+  int32_t reserved[6];
 } nomad_gpu_params;
 
 /* One rating set in either the reference's row-major file layout (row_counts !=
@@ -178,6 +183,12 @@ const char* nomad_gpu_last_error(void);
 
 /* 1 when a usable sm_103 device is present, else 0. */
 int nomad_gpu_device_ok(int32_t device);
+
+/* Tracing: for every column token, the seconds from the start of the most recent ASYNC
+ * nomad_gpu_epoch launch to the moment the token finished its last pass (0 for a
+ * column without training ratings).  `seconds` has n entries.  Shows which serial
+ * column chains set the epoch time.  NOMAD_ERR_UNSUPPORTED in other modes. */
+int nomad_gpu_token_finish_times(nomad_gpu_ctx* ctx, double* seconds);
 
 /* ---- evaluation without device allocation ---------------------------------------
  * No counterpart in the reference: it is an extra entry point for callers that

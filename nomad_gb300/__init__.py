@@ -208,6 +208,13 @@ class Nomad:
         H = None if H is None else np.ascontiguousarray(H, np.float32)
         check(lib().nomad_gpu_set_factors(self._ctx, _ptr(W), _ptr(H)), "nomad_gpu_set_factors")
 
+    def token_finish_times(self):
+        """Seconds from the last ASYNC epoch launch's start to each token's last pass."""
+        t = np.zeros(self.n, np.float64)
+        check(lib().nomad_gpu_token_finish_times(self._ctx, _ptr(t)),
+              "nomad_gpu_token_finish_times")
+        return t
+
     def info(self):
         i = _abi.Info()
         check(lib().nomad_gpu_get_info(self._ctx, ctypes.byref(i)), "nomad_gpu_get_info")

@@ -42,7 +42,8 @@ class Params(ctypes.Structure):
                 ("init", c_i32), ("init_parts", c_i32), ("device", c_i32), ("workers", c_i32),
                 ("warps_per_block", c_i32), ("blocks_per_sm", c_i32), ("balance", c_i32),
                 ("dsgd_inner_blocks", c_i32), ("dsgd_strategy", c_i32), ("exact", c_i32),
-                ("spin_budget_ms", c_i32), ("debug_flags", c_i32), ("reserved", c_i32 * 8)]
+                ("spin_budget_ms", c_i32), ("debug_flags", c_i32), ("long_visit", c_i32),
+                ("priority_permille", c_i32), ("reserved", c_i32 * 6)]
 
 
 class Matrix(ctypes.Structure):
@@ -102,6 +103,7 @@ SIGNATURES = {
     "nomad_gpu_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "nomad_gpu_last_error": (ctypes.c_char_p, []),
     "nomad_gpu_device_ok": (ctypes.c_int, [c_i32]),
+    "nomad_gpu_token_finish_times": (ctypes.c_int, [c_vp, c_vp]),
     "nomad_gpu_sse_noalloc": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,
                                              c_i64, c_i32, c_vp, c_vp]),
     "nomad_io_read_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_i32),

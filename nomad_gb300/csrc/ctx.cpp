@@ -37,6 +37,9 @@ struct nomad_gpu_ctx {
   int64_t* vl_ptr = nullptr;
   int32_t *tok_pos = nullptr, *tok_epoch = nullptr;
   int32_t *qnext = nullptr, *qtail = nullptr, *qnext0 = nullptr, *qtail0 = nullptr;
+  int4 *tok_desc = nullptr, *tok_desc0 = nullptr;
+  unsigned long long* finish_ns = nullptr;  // [n+1]: per-token retire time, [n] = launch start
+  int32_t n_priority = 0, long_visit = 14;
   int32_t* ctrl = nullptr;
   unsigned long long *progress = nullptr, *stats = nullptr;
   double* err_sum = nullptr;
@@ -202,9 +205,10 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   f.n = prob->n;
   f.dim = p.dim;
   f.bf16 = p.precision == NOMAD_PREC_BF16_SR;
-  const int E = f.bf16 ? 8 : 4;
-  f.kpad = (p.dim + E - 1) / E * E;
-  f.nvec = f.kpad / E;
+  // rows are whole 16-byte units (TMA bulk copies need it); a lane holds 4 values
+  const int align = f.bf16 ? 8 : 4;
+  f.kpad = (p.dim + align - 1) / align * align;
+  f.nvec = f.kpad / 4;
   if (f.nvec > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "dim %d exceeds the supported maximum", p.dim);
   f.red_width = 1;
   while (f.red_width < std::min(f.nvec, 32)) f.red_width <<= 1;
@@ -249,16 +253,30 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 8) : 8;
     const int nv = f.nvec <= 32 ? 1 : (f.nvec <= 64 ? 2 : 4);
     int bps = 0;
-    CK(nomad::async_occupancy(f.bf16, nv, p.exact, c->wpb, f.kpad, &bps));
+    if (p.exact)
+      CK(nomad::async_occupancy(f.bf16, nv, 1, c->wpb, f.kpad, &bps));
+    else
+      CK(nomad::async2_occupancy(f.bf16, nv, c->wpb, f.kpad, &bps));
     if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "async kernel does not fit on an SM");
     if (p.blocks_per_sm > 0) bps = std::min(bps, p.blocks_per_sm);
     const int64_t capacity = static_cast<int64_t>(bps) * c->num_sms * c->wpb;
     c->P = static_cast<int32_t>(p.workers > 0 ? std::min<int64_t>(p.workers, capacity) : capacity);
     c->grid = (c->P + c->wpb - 1) / c->wpb;
+    c->long_visit = p.long_visit > 0 ? p.long_visit : 14;
+    // columns whose serial chain is long enough to set the epoch time skip the queue
+    int64_t pri_min = 0;
+    if (!p.exact && p.priority_permille >= 0) {
+      const int permille = p.priority_permille > 0 ? p.priority_permille : 50;
+      pri_min = std::max<int64_t>(1, c->max_column * permille / 1000);
+    }
     nomad::AsyncLayout L;
-    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, L, threads));
+    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, L, threads));
     c->n_active = L.n_active;
+    c->n_priority = L.n_priority;
     c->n_segments = static_cast<int64_t>(L.segs.size());
+    RC(upload(c, &c->tok_desc0, reinterpret_cast<const int4*>(L.desc0.data()), L.desc0.size() / 4));
+    RC(dalloc(c, &c->tok_desc, std::max<size_t>(L.desc0.size() / 4, 1)));
+    RC(dalloc(c, &c->finish_ns, static_cast<size_t>(f.n) + 1));
     RC(upload(c, &c->segs, reinterpret_cast<const int4*>(L.segs.data()), L.segs.size()));
     RC(upload(c, &c->vl_ptr, L.vl_ptr.data(), L.vl_ptr.size()));
     RC(upload(c, &c->qnext0, L.qnext0.data(), L.qnext0.size()));
@@ -295,17 +313,22 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
 
 int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   const int32_t n = c->f.n;
-  const size_t qn = static_cast<size_t>(n) + c->P;
+  const size_t qn = static_cast<size_t>(n) + 2 * static_cast<size_t>(c->P);
   if (c->prm.debug_flags & 1) {
-    CK(nomad::launch_empty_queues(c->qnext, c->qtail, n, c->P, c->stream));
+    CK(nomad::launch_empty_queues(c->qnext, c->qtail, n, 2 * c->P, c->stream));
   } else {
     CK(cudaMemcpyAsync(c->qnext, c->qnext0, qn * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->qtail, c->qtail0, c->P * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->qtail, c->qtail0, 2 * static_cast<size_t>(c->P) * sizeof(int32_t),
+                       cudaMemcpyDeviceToDevice, c->stream));
   }
+  if (n > 0)
+    CK(cudaMemcpyAsync(c->tok_desc, c->tok_desc0, static_cast<size_t>(n) * sizeof(int4),
+                       cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemsetAsync(c->ctrl, 0, 4 * sizeof(int32_t), c->stream));
   CK(cudaMemsetAsync(c->progress, 0, sizeof(unsigned long long), c->stream));
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->stream));
   CK(cudaMemsetAsync(c->err_sum, 0, sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->finish_ns, 0, (static_cast<size_t>(n) + 1) * sizeof(unsigned long long), c->stream));
   nomad::AsyncArgs a;
   a.f = c->f;
   a.ratings = c->train;
@@ -313,6 +336,9 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.vl_ptr = c->vl_ptr;
   a.tok_pos = c->tok_pos;
   a.tok_epoch = c->tok_epoch;
+  a.tok_desc = c->tok_desc;
+  a.heavy_min = c->long_visit;
+  a.finish_ns = c->finish_ns;
   a.steps = c->steps;
   a.n_steps = c->n_steps;
   a.qnext = c->qnext;
@@ -331,7 +357,12 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.warps_per_block = c->wpb;
   a.grid = c->grid;
   CK(cudaEventRecord(c->ev0, c->stream));
-  if (c->n_active > 0) CK(nomad::launch_async(a, c->stream));
+  if (c->n_active > 0) {
+    if (c->prm.exact)
+      CK(nomad::launch_async(a, c->stream));
+    else
+      CK(nomad::launch_async2(a, c->stream));
+  }
   CK(cudaEventRecord(c->ev1, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   int32_t ctrl[4];
@@ -612,6 +643,22 @@ const char* nomad_gpu_strerror(int status) {
 }
 
 const char* nomad_gpu_last_error(void) { return nomad::last_error(); }
+
+int nomad_gpu_token_finish_times(nomad_gpu_ctx* c, double* seconds) {
+  nomad::clear_last_error();
+  if (!c || !seconds) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null argument");
+  if (c->prm.mode != NOMAD_MODE_ASYNC || !c->finish_ns)
+    NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "token finish times exist in ASYNC mode only");
+  CK(cudaSetDevice(c->device));
+  const int32_t n = c->f.n;
+  std::vector<unsigned long long> t(static_cast<size_t>(n) + 1);
+  CK(cudaMemcpy(t.data(), c->finish_ns, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  c->d2h_bytes += static_cast<int64_t>(t.size() * sizeof(unsigned long long));
+  const unsigned long long t0 = t[n];
+  for (int32_t j = 0; j < n; ++j)
+    seconds[j] = (t[j] && t0 && t[j] >= t0) ? static_cast<double>(t[j] - t0) * 1e-9 : 0.0;
+  return NOMAD_OK;
+}
 
 int nomad_gpu_device_ok(int32_t device) {
   int count = 0;

@@ -104,83 +104,68 @@ __device__ __forceinline__ uint32_t f32_to_bf16_sr_bits(float f, uint32_t r16) {
 __device__ __forceinline__ float bf16_bits_to_f32(uint32_t b) { return __uint_as_float(b << 16); }
 
 // ---- storage traits ---------------------------------------------------------------
-// A lane moves one 16-byte vector of a factor row: 4 fp32 or 8 bf16 values.
+// A lane moves one vector of 4 values of a factor row: 16 bytes of fp32 or 8 bytes of
+// bf16 ("Raw" is the packed form kept in registers while a row is in flight).
 template <typename Store>
 struct Vec;
 template <>
 struct Vec<float> {
   static constexpr int E = 4;
+  using Raw = uint4;
 };
 template <>
 struct Vec<__nv_bfloat16> {
-  static constexpr int E = 8;
+  static constexpr int E = 4;
+  using Raw = uint2;
 };
 
-template <typename Store>
-__device__ __forceinline__ void load_vec(const Store* row, int v, float (&x)[Vec<Store>::E]);
-template <>
-__device__ __forceinline__ void load_vec<float>(const float* row, int v, float (&x)[4]) {
-  const float4 q = reinterpret_cast<const float4*>(row)[v];
-  x[0] = q.x; x[1] = q.y; x[2] = q.z; x[3] = q.w;
+__device__ __forceinline__ void unpack(const uint4& q, float (&x)[4]) {
+  x[0] = __uint_as_float(q.x); x[1] = __uint_as_float(q.y);
+  x[2] = __uint_as_float(q.z); x[3] = __uint_as_float(q.w);
 }
-template <>
-__device__ __forceinline__ void load_vec<__nv_bfloat16>(const __nv_bfloat16* row, int v, float (&x)[8]) {
-  const uint4 q = reinterpret_cast<const uint4*>(row)[v];
-  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    x[2 * i] = __uint_as_float(w[i] << 16);
-    x[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-  }
+__device__ __forceinline__ void unpack(const uint2& q, float (&x)[4]) {
+  x[0] = __uint_as_float(q.x << 16); x[1] = __uint_as_float(q.x & 0xffff0000u);
+  x[2] = __uint_as_float(q.y << 16); x[3] = __uint_as_float(q.y & 0xffff0000u);
 }
-// L2-only (coherent) variants for data that other workers hand over (H rows).
-template <typename Store>
-__device__ __forceinline__ void load_vec_cg(const Store* row, int v, float (&x)[Vec<Store>::E]);
+template <typename Raw>
+__device__ __forceinline__ Raw zero_raw();
 template <>
-__device__ __forceinline__ void load_vec_cg<float>(const float* row, int v, float (&x)[4]) {
-  const float4 q = __ldcg(reinterpret_cast<const float4*>(row) + v);
-  x[0] = q.x; x[1] = q.y; x[2] = q.z; x[3] = q.w;
+__device__ __forceinline__ uint4 zero_raw<uint4>() { return make_uint4(0u, 0u, 0u, 0u); }
+template <>
+__device__ __forceinline__ uint2 zero_raw<uint2>() { return make_uint2(0u, 0u); }
+
+// fp32 values to the stored form; bf16 uses stochastic rounding keyed by `key`
+// (the caller makes keys distinct per row, update and vector).
+__device__ __forceinline__ uint4 pack_raw(const float (&x)[4], uint32_t, uint4*) {
+  return make_uint4(__float_as_uint(x[0]), __float_as_uint(x[1]), __float_as_uint(x[2]),
+                    __float_as_uint(x[3]));
 }
-template <>
-__device__ __forceinline__ void load_vec_cg<__nv_bfloat16>(const __nv_bfloat16* row, int v, float (&x)[8]) {
-  const uint4 q = __ldcg(reinterpret_cast<const uint4*>(row) + v);
-  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    x[2 * i] = __uint_as_float(w[i] << 16);
-    x[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-  }
+__device__ __forceinline__ uint2 pack_raw(const float (&x)[4], uint32_t key, uint2*) {
+  const uint32_t r0 = hash32(key), r1 = hash32(key + 1u);
+  const uint32_t a = f32_to_bf16_sr_bits(x[0], r0) & 0xffffu, b = f32_to_bf16_sr_bits(x[1], r0 >> 16);
+  const uint32_t c = f32_to_bf16_sr_bits(x[2], r1) & 0xffffu, d = f32_to_bf16_sr_bits(x[3], r1 >> 16);
+  return make_uint2(a | (b << 16), c | (d << 16));
 }
 
-// Store a vector; bf16 uses stochastic rounding keyed by `key` (lane-distinct).
+template <typename Store>
+__device__ __forceinline__ void load_vec(const Store* row, int v, float (&x)[4]) {
+  using Raw = typename Vec<Store>::Raw;
+  unpack(reinterpret_cast<const Raw*>(row)[v], x);
+}
+// L2-only (coherent) load for data other workers hand over (H rows).
+template <typename Store>
+__device__ __forceinline__ void load_vec_cg(const Store* row, int v, float (&x)[4]) {
+  using Raw = typename Vec<Store>::Raw;
+  unpack(__ldcg(reinterpret_cast<const Raw*>(row) + v), x);
+}
 template <typename Store, bool CG>
-__device__ __forceinline__ void store_vec(Store* row, int v, const float (&x)[Vec<Store>::E], uint32_t key);
-template <>
-__device__ __forceinline__ void store_vec<float, false>(float* row, int v, const float (&x)[4], uint32_t) {
-  reinterpret_cast<float4*>(row)[v] = make_float4(x[0], x[1], x[2], x[3]);
-}
-template <>
-__device__ __forceinline__ void store_vec<float, true>(float* row, int v, const float (&x)[4], uint32_t) {
-  __stcg(reinterpret_cast<float4*>(row) + v, make_float4(x[0], x[1], x[2], x[3]));
-}
-__device__ __forceinline__ uint4 pack_bf16_sr(const float (&x)[8], uint32_t key) {
-  uint32_t w[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const uint32_t r = hash32(key + static_cast<uint32_t>(i));
-    const uint32_t lo = f32_to_bf16_sr_bits(x[2 * i], r);
-    const uint32_t hi = f32_to_bf16_sr_bits(x[2 * i + 1], r >> 16);
-    w[i] = (lo & 0xffffu) | (hi << 16);
-  }
-  return make_uint4(w[0], w[1], w[2], w[3]);
-}
-template <>
-__device__ __forceinline__ void store_vec<__nv_bfloat16, false>(__nv_bfloat16* row, int v, const float (&x)[8], uint32_t key) {
-  reinterpret_cast<uint4*>(row)[v] = pack_bf16_sr(x, key);
-}
-template <>
-__device__ __forceinline__ void store_vec<__nv_bfloat16, true>(__nv_bfloat16* row, int v, const float (&x)[8], uint32_t key) {
-  __stcg(reinterpret_cast<uint4*>(row) + v, pack_bf16_sr(x, key));
+__device__ __forceinline__ void store_vec(Store* row, int v, const float (&x)[4], uint32_t key) {
+  using Raw = typename Vec<Store>::Raw;
+  const Raw q = pack_raw(x, key, static_cast<Raw*>(nullptr));
+  if (CG)
+    __stcg(reinterpret_cast<Raw*>(row) + v, q);
+  else
+    reinterpret_cast<Raw*>(row)[v] = q;
 }
 
 __device__ __forceinline__ float warp_allreduce(float v, int width) {

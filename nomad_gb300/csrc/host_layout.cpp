@@ -148,7 +148,7 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
 }
 
 int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
-                       AsyncLayout& L, int threads) {
+                       int64_t priority_min, AsyncLayout& L, int threads) {
   const int32_t m = csc.m, n = csc.n;
   const int64_t nnz = csc.nnz();
   if (P <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker count must be positive");
@@ -230,15 +230,25 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     if (nseg[j] > 0) ++L.n_active;
   }
   // initial queues: every active token at its first worker, in column order
-  // (nb_main.cpp:82-97 pushes the tokens in index order)
-  L.qnext0.assign(static_cast<size_t>(n) + P, -1);
-  L.qtail0.resize(P);
-  for (int32_t w = 0; w < P; ++w) L.qtail0[w] = n + w;
+  // (nb_main.cpp:82-97 pushes the tokens in index order); long columns go to the
+  // worker's priority queue (queue P + w)
+  L.qnext0.assign(static_cast<size_t>(n) + 2 * static_cast<size_t>(P), -1);
+  L.qtail0.resize(2 * static_cast<size_t>(P));
+  for (int32_t q = 0; q < 2 * P; ++q) L.qtail0[q] = n + q;
+  L.desc0.assign(4 * static_cast<size_t>(n), 0);
+  L.n_priority = 0;
   for (int32_t j = 0; j < n; ++j) {
     if (nseg[j] == 0) continue;
-    const int32_t w = L.segs[L.vl_ptr[j]].worker;
-    L.qnext0[L.qtail0[w]] = j;
-    L.qtail0[w] = j;
+    const Segment& s0 = L.segs[L.vl_ptr[j]];
+    const bool pri = priority_min > 0 && csc.col_ptr[j + 1] - csc.col_ptr[j] >= priority_min;
+    L.n_priority += pri ? 1 : 0;
+    const int32_t q = (pri ? P : 0) + s0.worker;
+    L.qnext0[L.qtail0[q]] = j;
+    L.qtail0[q] = j;
+    L.desc0[4 * static_cast<size_t>(j) + 0] = static_cast<int32_t>(static_cast<uint64_t>(s0.start) & 0xffffffffu);
+    L.desc0[4 * static_cast<size_t>(j) + 1] = static_cast<int32_t>(s0.start >> 32);
+    L.desc0[4 * static_cast<size_t>(j) + 2] = s0.len;
+    L.desc0[4 * static_cast<size_t>(j) + 3] = pri ? static_cast<int32_t>(0x80000000u) : 0;
   }
   return NOMAD_OK;
 }

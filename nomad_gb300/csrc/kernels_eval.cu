@@ -23,13 +23,10 @@ __device__ __forceinline__ float dot_vec<float>(const float* a, const float* b, 
 }
 template <>
 __device__ __forceinline__ float dot_vec<__nv_bfloat16>(const __nv_bfloat16* a, const __nv_bfloat16* b, int v) {
-  float x[8], y[8];
+  float x[4], y[4];
   nd::load_vec<__nv_bfloat16>(a, v, x);
   nd::load_vec_cg<__nv_bfloat16>(b, v, y);
-  float s = 0.f;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) s = fmaf(x[i], y[i], s);
-  return s;
+  return fmaf(x[0], y[0], fmaf(x[1], y[1], fmaf(x[2], y[2], x[3] * y[3])));
 }
 
 // Squared-error sum over a CSC rating set (the evaluation pass of
@@ -281,14 +278,14 @@ extern "C" int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t 
                "blocks = %d exceeds the fixed partial-sum array of %d blocks", blocks,
                NOMAD_NOALLOC_MAX_BLOCKS);
   const int bf16 = precision == NOMAD_PREC_BF16_SR;
-  const int E = bf16 ? 8 : 4;
+  const int align = bf16 ? 8 : 4;  // rows are whole 16-byte units
   nomad::DevFactors f;
   f.W = const_cast<void*>(W);
   f.H = const_cast<void*>(H);
   f.n = n;
   f.dim = dim;
-  f.kpad = (dim + E - 1) / E * E;
-  f.nvec = f.kpad / E;
+  f.kpad = (dim + align - 1) / align * align;
+  f.nvec = f.kpad / 4;
   f.bf16 = bf16;
   f.red_width = 32;
   if (f.nvec > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "dim %d exceeds the supported maximum", dim);

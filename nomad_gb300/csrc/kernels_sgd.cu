@@ -18,34 +18,17 @@ namespace {
 using nd::kFull;
 using nd::Vec;
 
-// Raw 16-byte vectors of a row (fp32 x4 or bf16 x8): kept packed while in flight so a
-// bf16 prefetch costs 4 registers per row, unpacked to fp32 when used.
-template <int NV>
-__device__ __forceinline__ void load_row_raw(const void* __restrict__ base, int r, int kpad_bytes,
-                                             int nvec, int lane, uint4 (&x)[NV]) {
-  const uint4* row = reinterpret_cast<const uint4*>(static_cast<const char*>(base) +
-                                                    static_cast<int64_t>(r) * kpad_bytes);
+// Raw vectors of a row (fp32 x4 = 16 bytes, bf16 x4 = 8 bytes): kept packed while in
+// flight, unpacked to fp32 when used.
+template <typename Store, int NV>
+__device__ __forceinline__ void load_row_raw(const Store* __restrict__ W, int r, int kpad, int nvec,
+                                             int lane, typename Vec<Store>::Raw (&x)[NV]) {
+  using Raw = typename Vec<Store>::Raw;
+  const Raw* row = reinterpret_cast<const Raw*>(W + static_cast<int64_t>(r) * kpad);
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const int v = lane + 32 * q;
-    x[q] = v < nvec ? row[v] : make_uint4(0u, 0u, 0u, 0u);
-  }
-}
-
-template <typename Store>
-__device__ __forceinline__ void unpack(const uint4& q, float (&x)[Vec<Store>::E]);
-template <>
-__device__ __forceinline__ void unpack<float>(const uint4& q, float (&x)[4]) {
-  x[0] = __uint_as_float(q.x); x[1] = __uint_as_float(q.y);
-  x[2] = __uint_as_float(q.z); x[3] = __uint_as_float(q.w);
-}
-template <>
-__device__ __forceinline__ void unpack<__nv_bfloat16>(const uint4& q, float (&x)[8]) {
-  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    x[2 * i] = __uint_as_float(w[i] << 16);
-    x[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+    x[q] = v < nvec ? row[v] : nd::zero_raw<Raw>();
   }
 }
 
@@ -53,10 +36,10 @@ template <typename Store, int NV>
 __device__ __forceinline__ void load_row(const Store* __restrict__ W, int r, int kpad,
                                          int nvec, int lane,
                                          float (&x)[NV][Vec<Store>::E]) {
-  uint4 raw[NV];
-  load_row_raw<NV>(W, r, kpad * static_cast<int>(sizeof(Store)), nvec, lane, raw);
+  typename Vec<Store>::Raw raw[NV];
+  load_row_raw<Store, NV>(W, r, kpad, nvec, lane, raw);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) unpack<Store>(raw[q], x[q]);
+  for (int q = 0; q < NV; ++q) nd::unpack(raw[q], x[q]);
 }
 
 template <typename Store, int NV>
@@ -140,12 +123,11 @@ __device__ __forceinline__ float visit_segment(Store* __restrict__ W, const noma
     const int cnt = min(32, len - base);
     int2 rv = make_int2(0, 0);
     if (lane < cnt) rv = __ldg(&ratings[start + base + lane]);
-    const int kb = f.kpad * static_cast<int>(sizeof(Store));
-    uint4 wbuf[PF][NV];
+    typename Vec<Store>::Raw wbuf[PF][NV];
 #pragma unroll
     for (int i = 0; i < PF; ++i) {
       const int r = __shfl_sync(kFull, rv.x, i);
-      if (i < cnt) load_row_raw<NV>(W, r, kb, f.nvec, lane, wbuf[i]);
+      if (i < cnt) load_row_raw<Store, NV>(W, r, f.kpad, f.nvec, lane, wbuf[i]);
     }
     for (int t0 = 0; t0 < cnt; t0 += PF) {
 #pragma unroll
@@ -156,7 +138,7 @@ __device__ __forceinline__ float visit_segment(Store* __restrict__ W, const noma
           const float v = __int_as_float(__shfl_sync(kFull, rv.y, t));
           float w[NV][Vec<Store>::E];
 #pragma unroll
-          for (int q = 0; q < NV; ++q) unpack<Store>(wbuf[i][q], w[q]);
+          for (int q = 0; q < NV; ++q) nd::unpack(wbuf[i][q], w[q]);
           const float err = rating_error<Store, NV, EXACT>(h, w, v, f.nvec, f.red_width, f.dim, lane, xbuf);
           seg_err += err * err;
           apply_update<Store, NV, EXACT>(h, w, err, step, lambda);
@@ -164,7 +146,7 @@ __device__ __forceinline__ float visit_segment(Store* __restrict__ W, const noma
                                nd::hash32(static_cast<uint32_t>(r) * 0x9E3779B1u ^ colkey));
           const int tn = t + PF;
           const int rn = __shfl_sync(kFull, rv.x, tn & 31);
-          if (tn < cnt) load_row_raw<NV>(W, rn, kb, f.nvec, lane, wbuf[i]);
+          if (tn < cnt) load_row_raw<Store, NV>(W, rn, f.kpad, f.nvec, lane, wbuf[i]);
         }
       }
     }

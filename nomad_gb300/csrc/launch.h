@@ -24,6 +24,7 @@ struct AsyncArgs {
   const int64_t* vl_ptr = nullptr;  // [n+1] visit list of each token
   int32_t* tok_pos = nullptr;       // [n]
   int32_t* tok_epoch = nullptr;     // [n]
+  int4* tok_desc = nullptr;         // [n] next visit {start lo, start hi, len, pos | heavy bit}
   const float* steps = nullptr;     // [n_steps] step size per pass count
   int32_t n_steps = 0;
   int32_t* qnext = nullptr;         // [n + P]
@@ -38,6 +39,8 @@ struct AsyncArgs {
   int64_t budget_ns = 0;
   int32_t exact = 0;
   int32_t warps_per_block = 0, grid = 0;
+  int32_t heavy_min = 14;  // visits with at least this many ratings take the blocked path
+  unsigned long long* finish_ns = nullptr;  // [n] globaltimer when each token retired
 };
 
 struct ReplayArgs {
@@ -77,6 +80,8 @@ struct SseArgs {
 cudaError_t launch_async(const AsyncArgs& a, cudaStream_t s);
 cudaError_t async_occupancy(int bf16, int nv, int exact, int warps_per_block, int kpad,
                             int* blocks_per_sm);
+cudaError_t launch_async2(const AsyncArgs& a, cudaStream_t s);
+cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int* blocks_per_sm);
 cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
 cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);

@@ -37,8 +37,10 @@ struct AsyncLayout {
   std::vector<int32_t> row_start;  // [P+1] first row of each worker's block
   std::vector<int64_t> vl_ptr;     // [n+1] visit list of each column
   std::vector<Segment> segs;       // visits, each column's list in its route order
-  std::vector<int32_t> qnext0;     // [n+P] initial queues (tokens in column order)
-  std::vector<int32_t> qtail0;     // [P]
+  std::vector<int32_t> qnext0;     // [n+2P] initial queues (tokens in column order)
+  std::vector<int32_t> qtail0;     // [2P]: queue w = worker w's queue, P+w its priority queue
+  std::vector<int32_t> desc0;      // [4n] first visit of each token {start lo, hi, len, 0|heavy}
+  int32_t n_priority = 0;          // tokens that use the priority queues
   int32_t n_active = 0;
   int64_t max_column = 0;
   int64_t max_segment = 0;
@@ -58,8 +60,10 @@ struct DsgdLayout {
 int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int threads);
 
 // Row blocks, visit lists (shuffled with `seed`) and the initial queues.
+// priority_min: columns with at least this many ratings use the priority queues
+// (<= 0: none).
 int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
-                       AsyncLayout& out, int threads);
+                       int64_t priority_min, AsyncLayout& out, int threads);
 
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
                       DsgdLayout& out);

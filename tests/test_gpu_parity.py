@@ -85,6 +85,29 @@ def test_async_one_worker_exact_equals_replay(ng, O, gpu_ok):
     assert np.array_equal(Wg, Wo) and np.array_equal(Hg, Ho), (relerr(Wg, Wo), relerr(Hg, Ho))
 
 
+@pytest.mark.parametrize("long_visit", [7, 1000])
+def test_async_one_worker_close_to_replay(ng, O, gpu_ok, long_visit):
+    """The pipelined kernel (FMA arithmetic, blocked 7-rating path for long visits,
+    algebraically equal to the reference update) against the nomad_float replay, with
+    one worker and no priority queue so the visit order is the replay's.  Tolerance:
+    1e-4 absolute per factor element (entries are ~0.1), 1e-5 relative on test RMSE."""
+    train, test = small_problem(ng, m=400, n=60, nnz_train=9000, nnz_test=900)
+    dim = 32
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=0.01, drate=DR, reg=REG,
+                  mode="async", workers=1, long_visit=long_visit,
+                  priority_permille=-1) as nm:
+        st = nm.epoch(3)
+        Wg, Hg = nm.factors()
+        rm = nm.rmse()[1]
+    assert st["updates"] == 3 * train.nnz
+    Wo, Ho = W0.copy(), H0.copy()
+    O.replay(train.to_csc(), Wo, Ho, 0, 3, 0.01, DR, REG)
+    assert np.max(np.abs(Wg - Wo)) <= 1e-4 and np.max(np.abs(Hg - Ho)) <= 1e-4
+    ref = O.rmse(test.to_csc(), Wo, Ho)
+    assert abs(rm - ref) <= 1e-5 * ref
+
+
 @pytest.mark.parametrize("workers", [0, 7, 64])
 def test_async_counts(ng, gpu_ok, workers):
     """Every rating is visited once per epoch (u=); one hop per (worker, column) visit."""
@@ -101,16 +124,18 @@ def test_async_counts(ng, gpu_ok, workers):
         assert info["workers"] == workers
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
-def test_async_rmse_vs_fp64_oracle(ng, O, gpu_ok, precision):
+@pytest.mark.parametrize("precision,workers", [("fp32", 0), ("bf16", 0), ("fp32", 8),
+                                               ("bf16", 8)])
+def test_async_rmse_vs_fp64_oracle(ng, O, gpu_ok, precision, workers):
     """10,000 x 2,000 workload, 20 epochs: test RMSE within 0.5% of the FP64 oracle
-    (nomad_double replay) at every epoch."""
+    (nomad_double replay) at every epoch.  With 8 workers the visits hold ~22 ratings,
+    so most of them run the blocked path."""
     train, test = ng.synth(1)
     dim, epochs = 100, 20
     W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
     gpu = []
     with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
-                  mode="async", precision=precision) as nm:
+                  mode="async", precision=precision, workers=workers) as nm:
         for _ in range(epochs):
             nm.epoch(1)
             gpu.append(nm.rmse()[1])

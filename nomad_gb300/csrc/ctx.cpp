@@ -38,6 +38,13 @@ struct nomad_gpu_ctx {
   int32_t *tok_pos = nullptr, *tok_epoch = nullptr;
   int32_t *qnext = nullptr, *qtail = nullptr, *qnext0 = nullptr, *qtail0 = nullptr;
   int4 *tok_desc = nullptr, *tok_desc0 = nullptr;
+  // pipelined kernel state
+  unsigned long long *ring_lo = nullptr, *ring_hi = nullptr;
+  unsigned mask_lo = 0, mask_hi = 0;
+  unsigned *tails = nullptr, *heads = nullptr;
+  int4 *mailbox = nullptr, *first_mail = nullptr;
+  int2* first_q = nullptr;
+  int32_t* q_count = nullptr;
   unsigned long long* finish_ns = nullptr;  // [n+1]: per-token retire time, [n] = launch start
   int32_t n_priority = 0, long_visit = 14;
   int32_t* ctrl = nullptr;
@@ -276,6 +283,25 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     c->n_segments = static_cast<int64_t>(L.segs.size());
     RC(upload(c, &c->tok_desc0, reinterpret_cast<const int4*>(L.desc0.data()), L.desc0.size() / 4));
     RC(dalloc(c, &c->tok_desc, std::max<size_t>(L.desc0.size() / 4, 1)));
+    if (!p.exact) {
+      // rings hold at most every token of their class at once
+      auto pow2 = [](int64_t x) { unsigned v = 2; while (v < x) v <<= 1; return v; };
+      c->mask_lo = pow2(static_cast<int64_t>(c->n_active) + 1) - 1;
+      c->mask_hi = pow2(static_cast<int64_t>(c->n_priority) + 1) - 1;
+      RC(dalloc(c, &c->ring_lo, static_cast<size_t>(c->P) * (c->mask_lo + 1)));
+      RC(dalloc(c, &c->ring_hi, static_cast<size_t>(c->P) * (c->mask_hi + 1)));
+      // all-ones entries never match a head (their token field has bit 31 set)
+      CK(cudaMemsetAsync(c->ring_lo, 0xff, static_cast<size_t>(c->P) * (c->mask_lo + 1) * 8, c->stream));
+      CK(cudaMemsetAsync(c->ring_hi, 0xff, static_cast<size_t>(c->P) * (c->mask_hi + 1) * 8, c->stream));
+      RC(dalloc(c, &c->tails, 2 * static_cast<size_t>(c->P)));
+      RC(dalloc(c, &c->heads, 2 * static_cast<size_t>(c->P)));
+      CK(cudaMemsetAsync(c->tails, 0, 2 * static_cast<size_t>(c->P) * sizeof(unsigned), c->stream));
+      CK(cudaMemsetAsync(c->heads, 0, 2 * static_cast<size_t>(c->P) * sizeof(unsigned), c->stream));
+      RC(dalloc(c, &c->mailbox, 2 * static_cast<size_t>(std::max(f.n, 1))));
+      RC(upload(c, &c->first_mail, reinterpret_cast<const int4*>(L.first_mail.data()), L.first_mail.size() / 4));
+      RC(upload(c, &c->first_q, reinterpret_cast<const int2*>(L.first_q.data()), L.first_q.size() / 2));
+      RC(upload(c, &c->q_count, L.q_count.data(), L.q_count.size()));
+    }
     RC(dalloc(c, &c->finish_ns, static_cast<size_t>(f.n) + 1));
     RC(upload(c, &c->segs, reinterpret_cast<const int4*>(L.segs.data()), L.segs.size()));
     RC(upload(c, &c->vl_ptr, L.vl_ptr.data(), L.vl_ptr.size()));
@@ -314,16 +340,16 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
 int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   const int32_t n = c->f.n;
   const size_t qn = static_cast<size_t>(n) + 2 * static_cast<size_t>(c->P);
-  if (c->prm.debug_flags & 1) {
-    CK(nomad::launch_empty_queues(c->qnext, c->qtail, n, 2 * c->P, c->stream));
-  } else {
-    CK(cudaMemcpyAsync(c->qnext, c->qnext0, qn * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->qtail, c->qtail0, 2 * static_cast<size_t>(c->P) * sizeof(int32_t),
-                       cudaMemcpyDeviceToDevice, c->stream));
+  const bool pipelined = !c->prm.exact;
+  if (!pipelined) {
+    if (c->prm.debug_flags & 1) {
+      CK(nomad::launch_empty_queues(c->qnext, c->qtail, n, 2 * c->P, c->stream));
+    } else {
+      CK(cudaMemcpyAsync(c->qnext, c->qnext0, qn * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->qtail, c->qtail0, 2 * static_cast<size_t>(c->P) * sizeof(int32_t),
+                         cudaMemcpyDeviceToDevice, c->stream));
+    }
   }
-  if (n > 0)
-    CK(cudaMemcpyAsync(c->tok_desc, c->tok_desc0, static_cast<size_t>(n) * sizeof(int4),
-                       cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemsetAsync(c->ctrl, 0, 4 * sizeof(int32_t), c->stream));
   CK(cudaMemsetAsync(c->progress, 0, sizeof(unsigned long long), c->stream));
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->stream));
@@ -339,6 +365,13 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.tok_desc = c->tok_desc;
   a.heavy_min = c->long_visit;
   a.finish_ns = c->finish_ns;
+  a.ring_lo = c->ring_lo;
+  a.ring_hi = c->ring_hi;
+  a.mask_lo = c->mask_lo;
+  a.mask_hi = c->mask_hi;
+  a.tails = c->tails;
+  a.heads = c->heads;
+  a.mailbox = c->mailbox;
   a.steps = c->steps;
   a.n_steps = c->n_steps;
   a.qnext = c->qnext;
@@ -356,6 +389,9 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.exact = c->prm.exact;
   a.warps_per_block = c->wpb;
   a.grid = c->grid;
+  // Seeding reads the ring geometry (a.P) and must follow every assignment above.
+  if (pipelined && !(c->prm.debug_flags & 1))
+    CK(nomad::launch_seed_queues(a, c->first_mail, c->first_q, c->q_count, n, c->epochs_done, c->stream));
   CK(cudaEventRecord(c->ev0, c->stream));
   if (c->n_active > 0) {
     if (c->prm.exact)
@@ -383,6 +419,10 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   }
   if (ctrl[1] != 0 || (c->n_active > 0 && ctrl[0] != c->n_active)) {
     RC(reset_tokens(c));
+    if (pipelined) {
+      CK(nomad::launch_drain_queues(a, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
     if (ctrl[1] == 2) NOMAD_FAIL(NOMAD_ERR_BOUNDS, "device bounds check failed");
     NOMAD_FAIL(NOMAD_ERR_TIMEOUT,
                "async epoch stopped: %d of %d tokens finished, no progress for %d ms",

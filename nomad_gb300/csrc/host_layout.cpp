@@ -236,6 +236,9 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
   L.qtail0.resize(2 * static_cast<size_t>(P));
   for (int32_t q = 0; q < 2 * P; ++q) L.qtail0[q] = n + q;
   L.desc0.assign(4 * static_cast<size_t>(n), 0);
+  L.first_mail.assign(8 * static_cast<size_t>(n), 0);
+  L.first_q.assign(2 * static_cast<size_t>(n), -1);
+  L.q_count.assign(2 * static_cast<size_t>(P), 0);
   L.n_priority = 0;
   for (int32_t j = 0; j < n; ++j) {
     if (nseg[j] == 0) continue;
@@ -249,6 +252,17 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     L.desc0[4 * static_cast<size_t>(j) + 1] = static_cast<int32_t>(s0.start >> 32);
     L.desc0[4 * static_cast<size_t>(j) + 2] = s0.len;
     L.desc0[4 * static_cast<size_t>(j) + 3] = pri ? static_cast<int32_t>(0x80000000u) : 0;
+    int32_t* fm = L.first_mail.data() + 8 * static_cast<size_t>(j);
+    fm[0] = static_cast<int32_t>(static_cast<uint64_t>(s0.start) & 0xffffffffu);
+    fm[1] = static_cast<int32_t>(s0.start >> 32);
+    fm[2] = s0.len;
+    fm[3] = 0;
+    fm[4] = 0;  // pass count, set per launch
+    fm[5] = static_cast<int32_t>(static_cast<uint32_t>(nseg[j]) | (pri ? 0x80000000u : 0u));
+    fm[6] = static_cast<int32_t>(static_cast<uint64_t>(L.vl_ptr[j]) & 0xffffffffu);
+    fm[7] = static_cast<int32_t>(L.vl_ptr[j] >> 32);
+    L.first_q[2 * static_cast<size_t>(j)] = q;
+    L.first_q[2 * static_cast<size_t>(j) + 1] = L.q_count[q]++;
   }
   return NOMAD_OK;
 }

@@ -41,6 +41,11 @@ struct AsyncLayout {
   std::vector<int32_t> qtail0;     // [2P]: queue w = worker w's queue, P+w its priority queue
   std::vector<int32_t> desc0;      // [4n] first visit of each token {start lo, hi, len, 0|heavy}
   int32_t n_priority = 0;          // tokens that use the priority queues
+  // pipelined kernel: first mailbox of each token (8 ints: start lo/hi, len, pos = 0;
+  // ep, nseg | heavy bit, vb lo/hi), its first queue and rank there, tokens per queue
+  std::vector<int32_t> first_mail;  // [8n]
+  std::vector<int32_t> first_q;     // [2n] {queue, rank}, queue -1 for an empty column
+  std::vector<int32_t> q_count;     // [2P]
   int32_t n_active = 0;
   int64_t max_column = 0;
   int64_t max_segment = 0;

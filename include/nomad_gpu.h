@@ -128,13 +128,16 @@ typedef struct nomad_gpu_info {
   int64_t nnz_train, nnz_test;
   int32_t workers;          /* ASYNC worker warps (REPLAY: 1)                      */
   int32_t active_tokens;    /* columns with at least one training rating          */
-  int64_t segments;         /* non-empty (worker, column) visits per epoch         */
+  int64_t segments;         /* visits per epoch: non-empty (worker, column) pairs, and
+                               (thread block, column) pairs of priority columns    */
   int64_t max_column;       /* largest column (ratings)                            */
   int32_t grid_blocks, block_threads, num_sms, inner_blocks;
   int64_t device_bytes;     /* device memory held by the context                   */
   int32_t mode, precision;
   int64_t h2d_bytes;        /* host-to-device bytes copied since init (cumulative) */
   int64_t d2h_bytes;        /* device-to-host bytes copied since init (cumulative) */
+  int32_t priority_tokens;  /* columns whose visits run on all warps of a block    */
+  int32_t reserved0;
 } nomad_gpu_info;
 
 typedef struct nomad_gpu_ctx nomad_gpu_ctx; /* opaque */

@@ -68,7 +68,8 @@ class Info(ctypes.Structure):
                 ("active_tokens", c_i32), ("segments", c_i64), ("max_column", c_i64),
                 ("grid_blocks", c_i32), ("block_threads", c_i32), ("num_sms", c_i32),
                 ("inner_blocks", c_i32), ("device_bytes", c_i64), ("mode", c_i32),
-                ("precision", c_i32), ("h2d_bytes", c_i64), ("d2h_bytes", c_i64)]
+                ("precision", c_i32), ("h2d_bytes", c_i64), ("d2h_bytes", c_i64),
+                ("priority_tokens", c_i32), ("reserved0", c_i32)]
 
 
 class IoMatrix(ctypes.Structure):

@@ -47,6 +47,7 @@ struct nomad_gpu_ctx {
   int32_t* q_count = nullptr;
   unsigned long long* finish_ns = nullptr;  // [n+1]: per-token retire time, [n] = launch start
   int32_t n_priority = 0, long_visit = 14;
+  int32_t cta_heavy = 0;  // priority tokens visit thread blocks (pipelined kernel)
   int32_t* ctrl = nullptr;
   unsigned long long *progress = nullptr, *stats = nullptr;
   double* err_sum = nullptr;
@@ -259,11 +260,13 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   if (p.mode == NOMAD_MODE_ASYNC) {
     c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 8) : 8;
     const int nv = f.nvec <= 32 ? 1 : (f.nvec <= 64 ? 2 : 4);
+    // pipelined kernel: long columns visit whole thread blocks (unless priority is off)
+    const int cta_heavy = !p.exact && p.priority_permille >= 0 ? 1 : 0;
     int bps = 0;
     if (p.exact)
       CK(nomad::async_occupancy(f.bf16, nv, 1, c->wpb, f.kpad, &bps));
     else
-      CK(nomad::async2_occupancy(f.bf16, nv, c->wpb, f.kpad, &bps));
+      CK(nomad::async2_occupancy(f.bf16, nv, c->wpb, f.kpad, cta_heavy, &bps));
     if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "async kernel does not fit on an SM");
     if (p.blocks_per_sm > 0) bps = std::min(bps, p.blocks_per_sm);
     const int64_t capacity = static_cast<int64_t>(bps) * c->num_sms * c->wpb;
@@ -277,7 +280,8 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       pri_min = std::max<int64_t>(1, c->max_column * permille / 1000);
     }
     nomad::AsyncLayout L;
-    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, L, threads));
+    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, cta_heavy ? c->wpb : 1, L, threads));
+    c->cta_heavy = cta_heavy && pri_min > 0;
     c->n_active = L.n_active;
     c->n_priority = L.n_priority;
     c->n_segments = static_cast<int64_t>(L.segs.size());
@@ -289,10 +293,10 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       c->mask_lo = pow2(static_cast<int64_t>(c->n_active) + 1) - 1;
       c->mask_hi = pow2(static_cast<int64_t>(c->n_priority) + 1) - 1;
       RC(dalloc(c, &c->ring_lo, static_cast<size_t>(c->P) * (c->mask_lo + 1)));
-      RC(dalloc(c, &c->ring_hi, static_cast<size_t>(c->P) * (c->mask_hi + 1)));
+      RC(dalloc(c, &c->ring_hi, static_cast<size_t>(c->grid) * (c->mask_hi + 1)));  // one per block
       // all-ones entries never match a head (their token field has bit 31 set)
       CK(cudaMemsetAsync(c->ring_lo, 0xff, static_cast<size_t>(c->P) * (c->mask_lo + 1) * 8, c->stream));
-      CK(cudaMemsetAsync(c->ring_hi, 0xff, static_cast<size_t>(c->P) * (c->mask_hi + 1) * 8, c->stream));
+      CK(cudaMemsetAsync(c->ring_hi, 0xff, static_cast<size_t>(c->grid) * (c->mask_hi + 1) * 8, c->stream));
       RC(dalloc(c, &c->tails, 2 * static_cast<size_t>(c->P)));
       RC(dalloc(c, &c->heads, 2 * static_cast<size_t>(c->P)));
       CK(cudaMemsetAsync(c->tails, 0, 2 * static_cast<size_t>(c->P) * sizeof(unsigned), c->stream));
@@ -372,6 +376,7 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.tails = c->tails;
   a.heads = c->heads;
   a.mailbox = c->mailbox;
+  a.cta_heavy = c->cta_heavy;
   a.steps = c->steps;
   a.n_steps = c->n_steps;
   a.qnext = c->qnext;
@@ -652,6 +657,8 @@ int nomad_gpu_get_info(nomad_gpu_ctx* c, nomad_gpu_info* info) {
   info->precision = c->prm.precision;
   info->h2d_bytes = c->h2d_bytes;
   info->d2h_bytes = c->d2h_bytes;
+  info->priority_tokens = c->cta_heavy ? c->n_priority : 0;
+  info->reserved0 = 0;
   return NOMAD_OK;
 }
 

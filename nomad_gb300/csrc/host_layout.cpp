@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <tuple>
 
 #include "layout.h"
 
@@ -148,10 +149,11 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
 }
 
 int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
-                       int64_t priority_min, AsyncLayout& L, int threads) {
+                       int64_t priority_min, int32_t group, AsyncLayout& L, int threads) {
   const int32_t m = csc.m, n = csc.n;
   const int64_t nnz = csc.nnz();
   if (P <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker count must be positive");
+  if (group <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker group size must be positive");
   L.P = P;
   L.row_start.assign(static_cast<size_t>(P) + 1, m);
   if (balance == 0 || nnz == 0) {
@@ -174,22 +176,33 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     }
     for (; w <= P; ++w) L.row_start[w] = m;
   }
-  // visit lists: the rows of a column are ascending, so each worker's share is a run
+  // visit lists: the rows of a column are ascending, so each worker's share is a run;
+  // a priority column's visits are the runs of whole worker groups
   L.vl_ptr.assign(static_cast<size_t>(n) + 1, 0);
   auto worker_of = [&](int32_t row) {
     return static_cast<int32_t>(std::upper_bound(L.row_start.begin(), L.row_start.end(), row) -
                                 L.row_start.begin()) - 1;
   };
+  auto is_priority = [&](int64_t j) {
+    return priority_min > 0 && csc.col_ptr[j + 1] - csc.col_ptr[j] >= priority_min;
+  };
+  // owner of `row` for column j: {worker or group index, first row past its block}
+  auto owner_of = [&](int32_t row, bool pri) {
+    const int32_t w = worker_of(row);
+    if (!pri) return std::make_pair(w, L.row_start[w + 1]);
+    const int32_t g = w / group;
+    return std::make_pair(g, L.row_start[std::min<int64_t>(static_cast<int64_t>(g + 1) * group, P)]);
+  };
   std::vector<int64_t> nseg(n, 0);
   parallel_chunks(n, threads, [&](int, int64_t lo, int64_t hi) {
     for (int64_t j = lo; j < hi; ++j) {
+      const bool pri = is_priority(j);
       int64_t c = 0;
       int32_t w = -1, wend = 0;
       for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
         const int32_t r = csc.ratings[o].row;
         if (w < 0 || r >= wend) {
-          w = worker_of(r);
-          wend = L.row_start[w + 1];
+          std::tie(w, wend) = owner_of(r, pri);
           ++c;
         }
       }
@@ -202,13 +215,13 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
   parallel_chunks(n, threads, [&](int t, int64_t lo, int64_t hi) {
     for (int64_t j = lo; j < hi; ++j) {
       Segment* s = L.segs.data() + L.vl_ptr[j];
+      const bool pri = is_priority(j);
       int64_t c = -1;
       int32_t w = -1, wend = 0;
       for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
         const int32_t r = csc.ratings[o].row;
         if (w < 0 || r >= wend) {
-          w = worker_of(r);
-          wend = L.row_start[w + 1];
+          std::tie(w, wend) = owner_of(r, pri);
           ++c;
           s[c] = Segment{o, 0, w};
         }
@@ -243,7 +256,7 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
   for (int32_t j = 0; j < n; ++j) {
     if (nseg[j] == 0) continue;
     const Segment& s0 = L.segs[L.vl_ptr[j]];
-    const bool pri = priority_min > 0 && csc.col_ptr[j + 1] - csc.col_ptr[j] >= priority_min;
+    const bool pri = is_priority(j);
     L.n_priority += pri ? 1 : 0;
     const int32_t q = (pri ? P : 0) + s0.worker;
     L.qnext0[L.qtail0[q]] = j;

@@ -41,14 +41,16 @@ struct AsyncArgs {
   int32_t warps_per_block = 0, grid = 0;
   int32_t heavy_min = 14;  // visits with at least this many ratings take the blocked path
   unsigned long long* finish_ns = nullptr;  // [n] globaltimer when each token retired
-  // ring queues of the pipelined kernel: worker w's normal ring is ring_lo[w*(mask_lo+1)..],
-  // its priority ring ring_hi[w*(mask_hi+1)..]; queue ids 0..P-1 normal, P..2P-1 priority
+  // ring queues of the pipelined kernel: worker w's ring is ring_lo[w*(mask_lo+1)..];
+  // thread block b's ring of priority tokens is ring_hi[b*(mask_hi+1)..]; queue ids
+  // 0..P-1 are worker rings, P+b block rings
   unsigned long long* ring_lo = nullptr;
   unsigned long long* ring_hi = nullptr;
   unsigned mask_lo = 0, mask_hi = 0;
   unsigned* tails = nullptr;  // [2P] producer counters
   unsigned* heads = nullptr;  // [2P] consumer counters
   int4* mailbox = nullptr;    // [2n] next visit of each token (two int4)
+  int32_t cta_heavy = 0;      // priority tokens visit thread blocks, whose warps process them together
 };
 
 struct ReplayArgs {
@@ -92,7 +94,7 @@ cudaError_t launch_async2(const AsyncArgs& a, cudaStream_t s);
 cudaError_t launch_seed_queues(const AsyncArgs& a, const int4* first_mail, const int2* first_q,
                                const int* counts, int n, int ep, cudaStream_t s);
 cudaError_t launch_drain_queues(const AsyncArgs& a, cudaStream_t s);
-cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int* blocks_per_sm);
+cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int cta_heavy, int* blocks_per_sm);
 cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
 cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);

@@ -108,6 +108,80 @@ def test_async_one_worker_close_to_replay(ng, O, gpu_ok, long_visit):
     assert abs(rm - ref) <= 1e-5 * ref
 
 
+@pytest.mark.parametrize("wpb,dim,precision", [(1, 32, "fp32"), (3, 100, "fp32"), (8, 100, "fp32"),
+                                               (8, 7, "fp32"), (8, 200, "fp32"), (8, 100, "bf16"),
+                                               (3, 7, "bf16"), (8, 200, "bf16")])
+def test_block_visits_close_to_replay(ng, O, gpu_ok, wpb, dim, precision):
+    """Every column on the priority route and one thread block of `wpb` warps: each visit
+    is a whole column, processed by the block's warps together in blocks of 32 ratings
+    (tensor-core Gram -- 3xTF32 for fp32 rows, bf16 products for bf16 rows -- and the
+    exact chain algebra), in the replay's FIFO column order.  Tolerance, fp32: 1e-4
+    absolute per factor element (entries are ~0.1) and 1e-5 relative on test RMSE; bf16
+    (stochastic rounding of every stored value): test RMSE within 0.5% of the replay's."""
+    train, test = small_problem(ng, m=400, n=60, nnz_train=9000, nnz_test=900)
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=0.01, drate=DR, reg=REG,
+                  mode="async", precision=precision, workers=wpb, warps_per_block=wpb,
+                  priority_permille=1) as nm:
+        info = nm.info()
+        st = nm.epoch(3)
+        Wg, Hg = nm.factors()
+        rm = nm.rmse()[1]
+    assert info["grid_blocks"] == 1
+    assert info["priority_tokens"] == info["active_tokens"] == train.n
+    assert st["updates"] == 3 * train.nnz and st["hops"] == 3 * train.n
+    Wo, Ho = W0.copy(), H0.copy()
+    O.replay(train.to_csc(), Wo, Ho, 0, 3, 0.01, DR, REG)
+    ref = O.rmse(test.to_csc(), Wo, Ho)
+    if precision == "fp32":
+        assert np.max(np.abs(Wg - Wo)) <= 1e-4 and np.max(np.abs(Hg - Ho)) <= 1e-4, \
+            (np.max(np.abs(Wg - Wo)), np.max(np.abs(Hg - Ho)))
+        assert abs(rm - ref) <= 1e-5 * ref
+    else:
+        assert abs(rm - ref) <= 5e-3 * ref, (rm, ref)
+
+
+@pytest.mark.parametrize("workers,wpb", [(64, 8), (40, 3)])
+def test_block_visits_mixed_counts(ng, gpu_ok, workers, wpb):
+    """Priority columns on block routes next to worker routes, several blocks (the last
+    one partly filled when workers % wpb != 0): every rating once per epoch."""
+    train, test = ng.synth(ng.synth_spec(2, m=3000, n=300, nnz_train=60000, nnz_test=2000,
+                                         seed=12345))
+    with ng.Nomad(train, test, dim=32, lrate=LR, drate=DR, reg=REG, mode="async",
+                  workers=workers, warps_per_block=wpb, priority_permille=100) as nm:
+        info = nm.info()
+        st = nm.epoch(2)
+    assert 0 < info["priority_tokens"] < info["active_tokens"]
+    assert info["grid_blocks"] == (workers + wpb - 1) // wpb
+    assert st["updates"] == 2 * train.nnz
+    assert st["hops"] == 2 * info["segments"]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_block_visits_mixed_rmse_vs_fp64_oracle(ng, O, gpu_ok, precision):
+    """A skewed 20,000 x 1,000 problem (the Netflix shape, scaled down) with its long
+    columns on block routes: test RMSE within 0.5% of the FP64 oracle at every epoch."""
+    train, test = ng.synth(ng.synth_spec(2, m=20000, n=1000, nnz_train=400000,
+                                         nnz_test=20000, seed=12345))
+    dim, epochs = 32, 10
+    W0, H0 = ng.reference_init(train.m, train.n, dim, 12345, 1)
+    gpu = []
+    with ng.Nomad(train, test, W0=W0, H0=H0, dim=dim, lrate=LR, drate=DR, reg=REG,
+                  mode="async", precision=precision, workers=256, warps_per_block=8) as nm:
+        assert 0 < nm.info()["priority_tokens"] < nm.info()["active_tokens"]
+        for _ in range(epochs):
+            nm.epoch(1)
+            gpu.append(nm.rmse()[1])
+    csc, tcsc = train.to_csc(), test.to_csc()
+    Wd, Hd = W0.astype(np.float64), H0.astype(np.float64)
+    ref = []
+    for e in range(epochs):
+        O.replay(csc, Wd, Hd, e, 1, LR, DR, REG)
+        ref.append(O.rmse(tcsc, Wd, Hd))
+    gap = np.abs(np.array(gpu) - np.array(ref)) / np.array(ref)
+    assert gap.max() <= 0.005, (gap.max(), gpu[-1], ref[-1])
+
+
 @pytest.mark.parametrize("workers", [0, 7, 64])
 def test_async_counts(ng, gpu_ok, workers):
     """Every rating is visited once per epoch (u=); one hop per (worker, column) visit."""

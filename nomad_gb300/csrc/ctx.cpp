@@ -43,6 +43,7 @@ struct nomad_gpu_ctx {
   unsigned mask_lo = 0, mask_hi = 0;
   unsigned *tails = nullptr, *heads = nullptr;
   int4 *mailbox = nullptr, *first_mail = nullptr;
+  int4* segx = nullptr;
   int2* first_q = nullptr;
   int32_t* q_count = nullptr;
   unsigned long long* finish_ns = nullptr;  // [n+1]: per-token retire time, [n] = launch start
@@ -178,7 +179,12 @@ int get_factor(nomad_gpu_ctx* c, const void* src, float* dst, int64_t rows) {
 
 int upload_csc(nomad_gpu_ctx* c, const nomad::Csc& csc, int2** ratings, int64_t** ptr) {
   RC(upload(c, ptr, csc.col_ptr.data(), csc.col_ptr.size()));
-  RC(upload(c, ratings, reinterpret_cast<const int2*>(csc.ratings.data()), csc.ratings.size()));
+  // two spare entries: 16-byte-rounded prefetches of a run may reach 8 bytes past its end
+  const size_t n = csc.ratings.size();
+  RC(dalloc(c, ratings, n + 2));
+  CK(cudaMemsetAsync(*ratings + n, 0, 2 * sizeof(int2), c->stream));
+  if (n) CK(cudaMemcpyAsync(*ratings, csc.ratings.data(), n * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+  c->h2d_bytes += static_cast<int64_t>(n * sizeof(int2));
   return NOMAD_OK;
 }
 
@@ -258,15 +264,26 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
 
   // ---- mode-specific layout --------------------------------------------------------
   if (p.mode == NOMAD_MODE_ASYNC) {
-    c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 8) : 8;
+    // exact kernel: up to 8 worker warps per block; pipelined kernel: up to 14 compute
+    // warps (workers) plus the pop and push warps
+    if (p.exact)
+      c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 8) : 8;
+    else
+      c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 14) : 14;
     const int nv = f.nvec <= 32 ? 1 : (f.nvec <= 64 ? 2 : 4);
     // pipelined kernel: long columns visit whole thread blocks (unless priority is off)
     const int cta_heavy = !p.exact && p.priority_permille >= 0 ? 1 : 0;
     int bps = 0;
-    if (p.exact)
+    if (p.exact) {
       CK(nomad::async_occupancy(f.bf16, nv, 1, c->wpb, f.kpad, &bps));
-    else
-      CK(nomad::async2_occupancy(f.bf16, nv, c->wpb, f.kpad, cta_heavy, &bps));
+    } else {
+      // fewer compute warps per block when long rows do not fit the shared memory
+      while (true) {
+        CK(nomad::async2_occupancy(f.bf16, nv, c->wpb, f.kpad, cta_heavy, &bps));
+        if (bps > 0 || c->wpb == 1) break;
+        --c->wpb;
+      }
+    }
     if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "async kernel does not fit on an SM");
     if (p.blocks_per_sm > 0) bps = std::min(bps, p.blocks_per_sm);
     const int64_t capacity = static_cast<int64_t>(bps) * c->num_sms * c->wpb;
@@ -301,13 +318,17 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       RC(dalloc(c, &c->heads, 2 * static_cast<size_t>(c->P)));
       CK(cudaMemsetAsync(c->tails, 0, 2 * static_cast<size_t>(c->P) * sizeof(unsigned), c->stream));
       CK(cudaMemsetAsync(c->heads, 0, 2 * static_cast<size_t>(c->P) * sizeof(unsigned), c->stream));
-      RC(dalloc(c, &c->mailbox, 2 * static_cast<size_t>(std::max(f.n, 1))));
+      RC(dalloc(c, &c->mailbox, 4 * static_cast<size_t>(std::max(f.n, 1))));
       RC(upload(c, &c->first_mail, reinterpret_cast<const int4*>(L.first_mail.data()), L.first_mail.size() / 4));
       RC(upload(c, &c->first_q, reinterpret_cast<const int2*>(L.first_q.data()), L.first_q.size() / 2));
       RC(upload(c, &c->q_count, L.q_count.data(), L.q_count.size()));
     }
     RC(dalloc(c, &c->finish_ns, static_cast<size_t>(f.n) + 1));
     RC(upload(c, &c->segs, reinterpret_cast<const int4*>(L.segs.data()), L.segs.size()));
+    if (!p.exact) {
+      RC(dalloc(c, &c->segx, 3 * std::max<size_t>(L.segs.size(), 1)));
+      CK(nomad::launch_build_segx(c->segs, c->train, static_cast<int64_t>(L.segs.size()), c->segx, c->stream));
+    }
     RC(upload(c, &c->vl_ptr, L.vl_ptr.data(), L.vl_ptr.size()));
     RC(upload(c, &c->qnext0, L.qnext0.data(), L.qnext0.size()));
     RC(upload(c, &c->qtail0, L.qtail0.data(), L.qtail0.size()));
@@ -376,6 +397,7 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.tails = c->tails;
   a.heads = c->heads;
   a.mailbox = c->mailbox;
+  a.segx = c->segx;
   a.cta_heavy = c->cta_heavy;
   a.steps = c->steps;
   a.n_steps = c->n_steps;
@@ -649,7 +671,7 @@ int nomad_gpu_get_info(nomad_gpu_ctx* c, nomad_gpu_info* info) {
   info->segments = c->n_segments;
   info->max_column = c->max_column;
   info->grid_blocks = c->grid;
-  info->block_threads = c->wpb * 32;
+  info->block_threads = (c->prm.mode == NOMAD_MODE_ASYNC && !c->prm.exact ? c->wpb + 2 : c->wpb) * 32;
   info->num_sms = c->num_sms;
   info->inner_blocks = c->innerB;
   info->device_bytes = c->device_bytes;

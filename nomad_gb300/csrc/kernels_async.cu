@@ -1,32 +1,33 @@
 // kernels_async.cu -- the pipelined asynchronous NOMAD kernel for sm_103a.
 //
-// Same algorithm as Code/nomad/nb_main.cpp:480-572: persistent worker warps own row
-// blocks, column tokens move between workers through per-worker queues, each visit runs
-// SGD over the (worker rows x column) ratings, and the step size of a visit follows the
-// token's pass count.  What makes a hop cheap on this GPU:
+// Same algorithm as Code/nomad/nb_main.cpp:480-572: persistent workers own row blocks,
+// column tokens move between workers through per-worker queues, each visit runs SGD over
+// the (worker rows x column) ratings, and the step size of a visit follows the token's
+// pass count.  What makes a hop cheap on this GPU:
 //
 //  1. Ring queues with sequence-tagged 64-bit entries.  A producer takes a slot with one
 //     atomic add and writes (sequence << 32 | token); a consumer owns its head counter and
 //     takes a token with one acquire load of the slot it expects.  Heads and tails never
-//     reset, so an entry left from an earlier pass can never match.  Each worker has a
-//     normal ring and a priority ring for long columns, whose serial chains set the epoch
-//     time; the worker drains the priority ring first.
-//  2. A per-token mailbox: the producer of a hop writes the next visit's descriptor (rating
-//     run, route position, pass count, route) next to the token, so the consumer needs no
-//     route lookups of its own.
-//  3. A four-stage token pipeline per warp.  A popped token's mailbox and held column are
-//     copied into a shared-memory slot by cp.async (stage D), then its rating indices
-//     (stage R), then its first rows are loaded (stage W), then it is processed.  Each
-//     stage's copies are issued one iteration before they are used.  The release fence of
-//     a hop comes right after the visit's stores and before the next copies are issued, so
-//     it waits only for those stores.
-//  4. Long visits run in blocks of 7 ratings with the chain rewritten exactly: with
+//     reset, so an entry left from an earlier pass can never match.
+//  2. Warp roles inside a thread block: compute warps (one per worker) only compute; a pop
+//     warp moves tokens from their rings into shared-memory inboxes, a push warp moves
+//     processed tokens from shared-memory outboxes into the rings behind one gpu-scope
+//     release fence per batch.  Compute warps synchronise at block scope only.
+//  3. A per-token mailbox: the producer of a hop writes the next visit (rating run, route
+//     position, pass count, route, first four ratings) next to the token, so the consumer
+//     can load its first rows as soon as the mailbox lands.
+//  4. A two-slot token pipeline per compute warp: a taken token's mailbox and held column
+//     are copied into shared memory by cp.async (D); next iteration its first rows are
+//     loaded into registers and its rating indices copied (W, R); then it is processed.
+//  5. Long visits run in blocks of 7 ratings with the chain rewritten exactly: with
 //     c = 1 - eta*lambda and b_j = <h_t, w_j> for the block's (distinct, old) rows,
 //        e_t = b_t - v_t,   b_j <- c b_j - eta e_t <w_t, w_j>   (j > t),
 //     so one reduce-scatter of the 7 <h, w_t> and 21 <w_s, w_t> replaces 7 dependent warp
 //     reductions; then w_t' = c w_t - eta e_t h_t and h_{t+1} = c h_t - eta e_t w_t are
 //     lane-local.  Rows are staged kRing-1 blocks ahead in shared memory by cp.async (a TMA
 //     bulk-copy variant is kept behind NOMAD_STAGE_TMA).
+//  6. Columns long enough to set the epoch time visit whole thread blocks instead of
+//     workers; the block's compute warps process such a visit together (below).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -44,7 +45,6 @@ constexpr int kPF = 4;       // rows prefetched in registers on the short-visit 
 constexpr int kBlk = 7;      // ratings per block on the long-visit path
 constexpr int kChunk = 28;   // ratings indexed per register chunk (4 blocks)
 constexpr int kRing = 3;     // staged blocks per warp on the long-visit path
-constexpr int kStages = 4;   // token pipeline slots (D, R, W, process)
 constexpr int kBarBytes = (8 * kRing + 15) / 16 * 16;  // mbarriers, padded to keep 16-byte alignment
 
 #ifndef NOMAD_STAGE_TMA
@@ -82,6 +82,11 @@ __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence
 __device__ __forceinline__ void fence_proxy_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+// Bulk prefetch of [p, p + bytes) into L2 (p and bytes multiples of 16).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
 // Per-lane asynchronous global -> shared copies (completion by commit groups).  The
 // 16-byte form bypasses L1 (.cg), so it also suits data that other SMs write.
@@ -109,17 +114,20 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
 }
 
 // ---- shared-memory slot of one pipelined token ----------------------------------------
-// Mailbox (32 bytes, written by the producer of the hop):
-//   a = {start lo, start hi, len, pos}        the visit's rating run and route position
+// Mailbox (64 bytes, written by the producer of the hop):
+//   a = {start lo, start hi, len, pos}           the visit's rating run and route position
 //   b = {ep, nseg | priority bit, vb lo, vb hi}  pass count, route length, route start
+//   c, d = the visit's first four ratings {row, value bits}
 struct SlotHdr {
   int4 a;
   int4 b;
-  int4 nxt;            // the route's next visit {start lo, start hi, len, worker}
+  int4 c;              // the visit's first ratings {r0, v0, r1, v1}
+  int4 d;              //                           {r2, v2, r3, v3}
+  int4 nxt[3];         // the route's next visit {start lo, start hi, len, worker} and its first ratings
   int4 pad;
   int2 rv[kChunk];     // the visit's first rating indices {row, value bits}
 };
-static_assert(sizeof(SlotHdr) == 64 + 8 * kChunk, "slot header layout");
+static_assert(sizeof(SlotHdr) == 128 + 8 * kChunk, "slot header layout");
 
 struct Shape {
   int nvec, red_width, row_bytes, heavy_min, slot_bytes;
@@ -152,19 +160,29 @@ __device__ __forceinline__ void load_row_regs(const void* W, int r, const Shape&
   }
 }
 
+// The visit's rating i < 4 as carried by the mailbox.
+__device__ __forceinline__ int2 first_rating(const SlotHdr* hd, int i) {
+  const int4 q = i < 2 ? hd->c : hd->d;
+  return (i & 1) ? make_int2(q.z, q.w) : make_int2(q.x, q.y);
+}
+
 // ---- short visit: one warp reduction per rating, rows kPF ahead in registers ----------
 template <typename Store, int NV>
-__device__ __forceinline__ float visit_short(const SlotHdr* hd, int len, typename Vec<Store>::Raw (&wb)[kPF][NV],
-                                             float (&h)[NV][Vec<Store>::E], void* W, const Shape& s, float step,
-                                             float lambda, uint32_t colkey, int lane) {
+__device__ __forceinline__ float visit_short(const SlotHdr* hd, int len, float (&h)[NV][Vec<Store>::E], void* W,
+                                             const Shape& s, float step, float lambda, uint32_t colkey, int lane) {
   constexpr int E = Vec<Store>::E;
+  using Raw = typename Vec<Store>::Raw;
+  Raw wb[kPF][NV];  // rows kPF ahead (the first ones were prefetched into L1 and L2)
+#pragma unroll
+  for (int i = 0; i < kPF; ++i)
+    if (i < len) load_row_regs<Store, NV>(W, first_rating(hd, i).x, s, lane, wb[i]);
   float err2 = 0.f;
   for (int t0 = 0; t0 < len; t0 += kPF) {
 #pragma unroll
     for (int i = 0; i < kPF; ++i) {
       const int t = t0 + i;
       if (t < len) {
-        const int2 rt = hd->rv[t];
+        const int2 rt = t0 == 0 ? first_rating(hd, i) : hd->rv[t];  // t0 == 0: t == i < 4
         float w[NV][E];
 #pragma unroll
         for (int q = 0; q < NV; ++q) nd::unpack(wb[i][q], w[q]);
@@ -423,8 +441,8 @@ constexpr int kCtaHdrBytes = 16;
 
 struct CtaHdr {
   int hv_tok;                // priority token the block processes next (-1: none)
-  int pad;
-  unsigned long long join;   // mbarrier, one arrival per live warp
+  int stop;                  // the launch is over (every token retired, or an error)
+  unsigned long long join;   // mbarrier, one arrival per live compute warp
 };
 static_assert(sizeof(CtaHdr) == kCtaHdrBytes, "block header layout");
 
@@ -763,8 +781,8 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
   const int tid = wib * 32 + lane;
   const int nthr = nw * 32;
   const int kpad = s.row_bytes / static_cast<int>(sizeof(Store));
-  const int4 ma = __ldcg(a.mailbox + 2 * static_cast<int64_t>(tok));
-  const int4 mb = __ldcg(a.mailbox + 2 * static_cast<int64_t>(tok) + 1);
+  const int4 ma = __ldcg(a.mailbox + 4 * static_cast<int64_t>(tok));
+  const int4 mb = __ldcg(a.mailbox + 4 * static_cast<int64_t>(tok) + 1);
   const int64_t start = lo_hi(ma.x, ma.y);
   const int len = ma.z, pos = ma.w, ep = mb.x;
   const int nblk = (len + kHB - 1) / kHB;
@@ -847,25 +865,22 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
 }
 
 // ---- stages of the token pipeline -------------------------------------------------------
-// D: the mailbox and the held column, into the token's slot.
-__device__ __forceinline__ void stage_d(char* slot, int tok, const nomad::AsyncArgs& a, int row_bytes, int lane) {
-  const uint32_t d = smem_u32(slot);
-  if (lane < 2) cp16(d + 16 * lane, reinterpret_cast<const char*>(a.mailbox + 2 * static_cast<int64_t>(tok) + lane));
-  const char* hrow = static_cast<const char*>(a.f.H) + static_cast<int64_t>(tok) * row_bytes;
-  const uint32_t hd = d + static_cast<uint32_t>(sizeof(SlotHdr));
-  for (int v = lane; v * 16 < row_bytes; v += 32) cp16(hd + 16 * v, hrow + 16 * v);
-}
-// R: needs the mailbox -- the visit's rating indices and the route's next visit.
-__device__ __forceinline__ void stage_r(char* slot, const nomad::AsyncArgs& a, int lane) {
+// D (issued by the pop warp): the mailbox and the held column, into an inbox slot.
+// R (compute warp): needs the mailbox -- the visit's rating indices when it holds more
+// ratings than the mailbox carries, and the route's next visit with its first ratings
+// (they go into the next hop's mailbox).
+__device__ __forceinline__ void stage_r(char* slot, const nomad::AsyncArgs& a, int heavy_min, int lane) {
   const SlotHdr* hd = reinterpret_cast<const SlotHdr*>(slot);
   const int4 ma = hd->a, mb = hd->b;
   const int64_t start = lo_hi(ma.x, ma.y);
   const uint32_t d = smem_u32(slot);
-  if (lane < min(ma.z, kChunk)) cp8(d + static_cast<uint32_t>(offsetof(SlotHdr, rv)) + 8 * lane, a.ratings + start + lane);
-  if (lane == 0) {
+  const int nidx = ma.z > kPF || ma.z >= heavy_min ? min(ma.z, kChunk) : 0;
+  if (lane < nidx) cp8(d + static_cast<uint32_t>(offsetof(SlotHdr, rv)) + 8 * lane, a.ratings + start + lane);
+  if (lane >= 29) {
     const int nseg = mb.y & 0x7fffffff;
     const int npos = ma.w + 1 < nseg ? ma.w + 1 : 0;
-    cp16(d + static_cast<uint32_t>(offsetof(SlotHdr, nxt)), a.segs + lo_hi(mb.z, mb.w) + npos);
+    const int k = lane - 29;
+    cp16(d + static_cast<uint32_t>(offsetof(SlotHdr, nxt)) + 16 * k, a.segx + 3 * (lo_hi(mb.z, mb.w) + npos) + k);
   }
 }
 
@@ -873,97 +888,332 @@ __device__ __forceinline__ bool entry_valid(unsigned long long e, unsigned head)
   return static_cast<unsigned>(e >> 32) == head && (e & 0x80000000ull) == 0;
 }
 
+// ---- hand-off between the warps of a block ---------------------------------------------
+// Compute warps touch no global queue: the pop warp moves tokens from each compute warp's
+// ring into its inbox -- an entry plus a slot that a bulk copy fills with the token's
+// mailbox and held column -- and the push warp moves processed tokens from the outboxes
+// into the rings, one gpu-scope release fence per batch.  Entries carry the producer's
+// count in their high word, so a slot holds a new entry when that count is the one
+// expected.  A compute warp frees an inbox slot when its token's visit is done.
+constexpr int kInbox = 8;
+constexpr int kOutbox = 8;
+
+struct WarpBox {
+  unsigned long long inbox[kInbox];       // (count << 32) | token, written by the pop warp
+  unsigned long long outbox[kOutbox][2];  // (count << 32) | token, then (queue << 1) | retire
+  unsigned long long bars[kInbox];        // mbarrier of each inbox slot's copy
+  unsigned in_head;                       // inbox slots the compute warp has freed
+  unsigned out_head;                      // outbox entries the push warp has published
+  unsigned pad[2];
+};
+static_assert(sizeof(WarpBox) == 272, "box layout");
+constexpr int kBoxWords = sizeof(WarpBox) / 8;
+constexpr int kBoxBarWord = offsetof(WarpBox, bars) / 8;       // initialised as mbarriers
+constexpr int kBoxCountWord = offsetof(WarpBox, in_head) / 8;  // counters start at zero
+
+__device__ __forceinline__ unsigned long long ld_acquire_cta_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.cta.shared::cta.b64 %0, [%1];" : "=l"(v) : "r"(smem_u32(p)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_cta_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+
+// A processed token into the warp's outbox (lane 0): qr = (queue << 1) | retire.  Waits
+// (bounded) for room; false when the launch is stopping or the wait ran out.
+__device__ __forceinline__ bool outbox_put(WarpBox& B, unsigned& out_tail, int tok, unsigned qr, const CtaHdr* hdr,
+                                           const nomad::AsyncArgs& a) {
+  if (out_tail - ld_acquire_cta_u32(&B.out_head) >= static_cast<unsigned>(kOutbox)) {
+    const uint64_t t0 = nd::globaltimer();
+    while (out_tail - ld_acquire_cta_u32(&B.out_head) >= static_cast<unsigned>(kOutbox)) {
+      __nanosleep(64);
+      if (ld_volatile_shared(&hdr->stop)) return false;
+      if (static_cast<int64_t>(nd::globaltimer() - t0) > a.budget_ns) {
+        atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
+        return false;
+      }
+    }
+  }
+  unsigned long long* e = B.outbox[out_tail % kOutbox];
+  e[1] = qr;
+  st_release_cta_u64(&e[0], (static_cast<unsigned long long>(out_tail) << 32) | static_cast<unsigned>(tok));
+  ++out_tail;
+  return true;
+}
+
+// The pop warp: lane i < nc fills compute warp i's inbox from its ring (two probes per
+// round); lane 31 takes the block's priority tokens.  Lane 0 also watches for the end of
+// the launch (every token retired, an error, or no progress within the budget) and raises
+// the block's stop flag.
+__device__ void pop_warp(const nomad::AsyncArgs& a, CtaHdr* hdr, WarpBox* boxes, char* slots_all, int slot_bytes,
+                         int row_bytes, int ncw, int nc_live, int lane) {
+  const int P = a.P;
+  const int w0 = static_cast<int>(blockIdx.x) * ncw;
+  const bool mine = lane < nc_live;
+  const bool heavy_lane = a.cta_heavy && lane == 31;
+  unsigned long long* ring = nullptr;
+  unsigned mask = 0, head = 0;
+  if (mine) {
+    ring = a.ring_lo + static_cast<int64_t>(w0 + lane) * (a.mask_lo + 1);
+    mask = a.mask_lo;
+    head = a.heads[w0 + lane];
+  } else if (heavy_lane) {
+    ring = a.ring_hi + static_cast<int64_t>(blockIdx.x) * (a.mask_hi + 1);
+    mask = a.mask_hi;
+    head = a.heads[P + blockIdx.x];
+  }
+  unsigned in_tail = 0;  // inboxes start empty every launch
+  unsigned long long seen = ~0ull;
+  uint64_t idle_since = nd::globaltimer();
+  unsigned backoff = 32, rounds = 0;
+  while (true) {
+    unsigned long long p0 = ~0ull, p1 = ~0ull;
+    if (ring) {
+      p0 = ld_acquire_u64(ring + (head & mask));
+      if (mine) p1 = ld_acquire_u64(ring + ((head + 1) & mask));
+    }
+    int took = 0;
+    if (mine) {
+      WarpBox& B = boxes[lane];
+      const unsigned used = in_tail - ld_acquire_cta_u32(&B.in_head);  // freed slots: their reads are done
+      if (used < static_cast<unsigned>(kInbox) && entry_valid(p0, head)) {
+        fence_proxy_async_global();  // the acquired mailbox and column, for the bulk copies
+        fence_proxy_async_shared();  // the slot's earlier generic reads precede the copy's writes
+        const int ntake = used + 1 < static_cast<unsigned>(kInbox) && entry_valid(p1, head + 1) ? 2 : 1;
+        for (int i = 0; i < ntake; ++i) {
+          const unsigned tok = static_cast<unsigned>((i ? p1 : p0) & 0x7fffffffull);
+          const int sl = static_cast<int>(in_tail % kInbox);
+          char* slot = slots_all + (static_cast<size_t>(lane) * kInbox + sl) * slot_bytes;
+          const uint32_t bar = smem_u32(&B.bars[sl]);
+          mbar_expect_tx(bar, static_cast<uint32_t>(64 + row_bytes));
+          tma_row(smem_u32(slot), a.mailbox + 4 * static_cast<int64_t>(tok), 64u, bar);
+          tma_row(smem_u32(slot + sizeof(SlotHdr)), static_cast<const char*>(a.f.H) + static_cast<int64_t>(tok) * row_bytes,
+                  static_cast<uint32_t>(row_bytes), bar);
+          st_release_cta_u64(&B.inbox[sl], (static_cast<unsigned long long>(in_tail) << 32) | tok);
+          ++in_tail;
+          ++head;
+        }
+        took = ntake;
+      }
+    } else if (heavy_lane) {
+      if (ld_acquire_cta_u32(reinterpret_cast<const unsigned*>(&hdr->hv_tok)) == 0xffffffffu && entry_valid(p0, head)) {
+        st_release_cta_u32(reinterpret_cast<unsigned*>(&hdr->hv_tok), static_cast<unsigned>(p0 & 0x7fffffffull));
+        ++head;
+        took = 1;
+      }
+    }
+    const bool any = __any_sync(kFull, took != 0);
+    int stop = 0;
+    if (lane == 0 && (!any || (++rounds & 15) == 0)) {
+      if (nd::ld_acquire(&a.ctrl[1]) != 0 || nd::ld_acquire(&a.ctrl[0]) >= a.n_active) {
+        stop = 1;
+      } else {
+        const unsigned long long pr = nd::ld_relaxed_u64(a.progress);
+        const uint64_t now = nd::globaltimer();
+        if (pr != seen) {
+          seen = pr;
+          idle_since = now;
+        } else if (static_cast<int64_t>(now - idle_since) > a.budget_ns) {
+          atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
+          stop = 1;
+        }
+      }
+      if (stop) st_volatile_shared(&hdr->stop, 1);
+    }
+    if (__shfl_sync(kFull, stop, 0)) break;
+    if (any) {
+      backoff = 32;
+    } else {
+      __nanosleep(backoff);
+      backoff = min(backoff * 2, 256u);
+    }
+  }
+  if (mine) {
+    a.heads[w0 + lane] = head;
+    // copies still in flight land before the block's shared memory goes away (bounded)
+    WarpBox& B = boxes[lane];
+    for (unsigned c = in_tail > kInbox ? in_tail - kInbox : 0u; c < in_tail; ++c)
+      for (int it = 0; it < (1 << 16) && !mbar_try_wait(smem_u32(&B.bars[c % kInbox]), (c / kInbox) & 1u); ++it) {
+      }
+  } else if (heavy_lane) {
+    a.heads[P + blockIdx.x] = head;
+  }
+}
+
+// The push warp: lane i < nc publishes up to four entries of compute warp i's outbox per
+// round, after one release fence of the whole warp (cumulative over the compute warps'
+// stores, which the outbox acquire ordered before it).
+__device__ void push_warp(const nomad::AsyncArgs& a, const CtaHdr* hdr, WarpBox* boxes, int nc_live, int lane) {
+  const int P = a.P;
+  const bool mine = lane < nc_live;
+  unsigned out_head = 0;
+  unsigned pend = 0;  // published hops not yet added to the progress counter
+  unsigned backoff = 32;
+  while (true) {
+    int n = 0;
+    unsigned tok[4], qr[4];
+    if (mine) {
+      WarpBox& B = boxes[lane];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        tok[k] = 0;
+        qr[k] = 0;
+        if (n == k) {
+          const unsigned long long* e = B.outbox[(out_head + k) % kOutbox];
+          const unsigned long long e0 = ld_acquire_cta_u64(&e[0]);
+          if (static_cast<unsigned>(e0 >> 32) == out_head + k) {
+            tok[k] = static_cast<unsigned>(e0) & 0x7fffffffu;
+            qr[k] = static_cast<unsigned>(e[1]);
+            n = k + 1;
+          }
+        }
+      }
+    }
+    if (__any_sync(kFull, n > 0)) {
+      fence_acq_rel_gpu();
+      unsigned seq[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < n && !(qr[k] & 1u)) seq[k] = atomicAdd(&a.tails[qr[k] >> 1], 1u);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k >= n) continue;
+        if (qr[k] & 1u) {
+          if (a.finish_ns) a.finish_ns[tok[k]] = nd::globaltimer();
+          atomicAdd(&a.ctrl[0], 1);
+        } else {
+          const int q = static_cast<int>(qr[k] >> 1);
+          unsigned long long* rq = q >= P ? a.ring_hi + static_cast<int64_t>(q - P) * (a.mask_hi + 1) + (seq[k] & a.mask_hi)
+                                          : a.ring_lo + static_cast<int64_t>(q) * (a.mask_lo + 1) + (seq[k] & a.mask_lo);
+          st_relaxed_u64(rq, (static_cast<unsigned long long>(seq[k]) << 32) | tok[k]);
+        }
+      }
+      if (n > 0) {
+        out_head += static_cast<unsigned>(n);
+        st_release_cta_u32(&boxes[lane].out_head, out_head);
+        pend += static_cast<unsigned>(n);
+        if (pend >= 64) {
+          atomicAdd(a.progress, static_cast<unsigned long long>(pend));
+          pend = 0;
+        }
+      }
+      backoff = 32;
+    } else {
+      if (ld_volatile_shared(&hdr->stop)) break;
+      __nanosleep(backoff);
+      backoff = min(backoff * 2, 256u);
+    }
+  }
+  if (pend) atomicAdd(a.progress, static_cast<unsigned long long>(pend));
+}
+
 template <typename Store, int NV>
-__global__ void __launch_bounds__(256, 2) nomad_async2_kernel(nomad::AsyncArgs a) {
+__global__ void __launch_bounds__(512, 1) nomad_async2_kernel(nomad::AsyncArgs a) {
   constexpr int E = Vec<Store>::E;
   using Raw = typename Vec<Store>::Raw;
   extern __shared__ __align__(128) char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int w = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int ncw = static_cast<int>(blockDim.x >> 5) - 2;  // compute warps (workers) per block
   const int P = a.P;
+  const int nc_live = min(ncw, P - static_cast<int>(blockIdx.x) * ncw);
   Shape s;
   s.nvec = a.f.nvec;
   s.red_width = a.f.red_width;
   s.row_bytes = a.f.kpad * static_cast<int>(sizeof(Store));
   s.heavy_min = min(max(a.heavy_min, 1), kChunk + 1);  // longer visits always take the blocked path
   s.slot_bytes = static_cast<int>(sizeof(SlotHdr)) + s.row_bytes;
-  // shared memory: block header | every warp's token slots | long-visit rings (the block
-  // visit region aliases them) | mbarriers | gather buffers
-  const int nwarps = blockDim.x >> 5;
-  const int nw_live = min(nwarps, P - static_cast<int>(blockIdx.x) * nwarps);
+  // shared memory: block header | boxes | inbox slots | long-visit rings (the block visit
+  // region aliases them) | mbarriers | gather buffers; per compute warp where repeated
   const size_t ring_bytes = static_cast<size_t>(kRing) * kBlk * s.row_bytes;
-  size_t region_bytes = static_cast<size_t>(nwarps) * ring_bytes;
+  size_t region_bytes = static_cast<size_t>(ncw) * ring_bytes;
   if (a.cta_heavy) region_bytes = max(region_bytes, cta_region_bytes(a.f.kpad, static_cast<int>(sizeof(Store))));
   CtaHdr* hdr = reinterpret_cast<CtaHdr*>(smem);
-  char* region = smem + kCtaHdrBytes + static_cast<size_t>(nwarps) * kStages * s.slot_bytes;
+  WarpBox* boxes = reinterpret_cast<WarpBox*>(smem + kCtaHdrBytes);
+  char* slots_all = reinterpret_cast<char*>(boxes + ncw);
+  char* region = slots_all + static_cast<size_t>(ncw) * kInbox * s.slot_bytes;
   char* bars = region + region_bytes;
-  char* slots = smem + kCtaHdrBytes + static_cast<size_t>(wib) * kStages * s.slot_bytes;
-  Ring R;
-  R.rows = region + static_cast<size_t>(wib) * ring_bytes;
-  R.bars = smem_u32(bars + static_cast<size_t>(wib) * kBarBytes);
-  R.gather = reinterpret_cast<float*>(bars + static_cast<size_t>(nwarps) * kBarBytes + static_cast<size_t>(wib) * 128);
-  R.phase = 0;
-  if (lane == 0 && NOMAD_STAGE_TMA)
-    for (int i = 0; i < kRing; ++i) mbar_init(R.bars + 8u * i, 1);
+  char* gathers = bars + static_cast<size_t>(ncw) * kBarBytes;
+  for (int i = threadIdx.x; i < ncw * kBoxWords; i += blockDim.x) {
+    const int wd = i % kBoxWords;
+    if (wd >= kBoxCountWord) reinterpret_cast<unsigned long long*>(boxes)[i] = 0ull;
+    else if (wd >= kBoxBarWord) mbar_init(smem_u32(reinterpret_cast<unsigned long long*>(boxes) + i), 1);
+    else reinterpret_cast<unsigned long long*>(boxes)[i] = ~0ull;
+  }
   const uint32_t join_bar = smem_u32(&hdr->join);
   if (threadIdx.x == 0) {
     hdr->hv_tok = -1;
-    if (nw_live > 0) mbar_init(join_bar, static_cast<uint32_t>(nw_live));
+    hdr->stop = 0;
+    mbar_init(join_bar, static_cast<uint32_t>(max(nc_live, 1)));
   }
+  Ring R;
+  R.rows = region + static_cast<size_t>(min(wib, ncw - 1)) * ring_bytes;
+  R.bars = smem_u32(bars + static_cast<size_t>(min(wib, ncw - 1)) * kBarBytes);
+  R.gather = reinterpret_cast<float*>(gathers + static_cast<size_t>(min(wib, ncw - 1)) * 128);
+  R.phase = 0;
+  if (lane == 0 && NOMAD_STAGE_TMA && wib < ncw)
+    for (int i = 0; i < kRing; ++i) mbar_init(R.bars + 8u * i, 1);
   fence_mbar_init();
   __syncthreads();
-  if (w >= P) return;
-  if (w == 0 && lane == 0 && a.finish_ns) a.finish_ns[a.f.n] = nd::globaltimer();
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.finish_ns) a.finish_ns[a.f.n] = nd::globaltimer();
+  if (wib == ncw) {
+    pop_warp(a, hdr, boxes, slots_all, s.slot_bytes, s.row_bytes, ncw, nc_live, lane);
+    return;
+  }
+  if (wib == ncw + 1) {
+    push_warp(a, hdr, boxes, nc_live, lane);
+    return;
+  }
+  if (wib >= nc_live) return;
+  // ---- a compute warp ----------------------------------------------------------------
   void* W = a.f.W;
-  const bool leader = wib == 0 && a.cta_heavy;  // polls the block's ring of priority tokens
+  WarpBox& B = boxes[wib];
+  char* slots = slots_all + static_cast<size_t>(wib) * kInbox * s.slot_bytes;
+  const bool leader = wib == 0 && a.cta_heavy;  // finishes the block's priority visits
   CtaRegion C = cta_region(region, a.f.kpad, static_cast<int>(sizeof(Store)));
   uint32_t join_phase = 0;
-  bool hv_held = false;
-  unsigned long long* my_lo = a.ring_lo + static_cast<int64_t>(w) * (a.mask_lo + 1);
-  unsigned long long* my_hi = a.ring_hi + static_cast<int64_t>(blockIdx.x) * (a.mask_hi + 1);
-  unsigned head_lo = 0, head_hi = 0;  // consumer counters (lane 0)
-  unsigned long long probe_lo = ~0ull, probe_hi = ~0ull;
-  if (lane == 0) {
-    head_lo = a.heads[w];
-    probe_lo = ld_acquire_u64(my_lo + (head_lo & a.mask_lo));
-    if (leader) {
-      head_hi = a.heads[P + blockIdx.x];
-      probe_hi = ld_acquire_u64(my_hi + (head_hi & a.mask_hi));
-    }
-  }
-  unsigned long long n_upd = 0, n_hops = 0, n_fail = 0, pending = 0, seen = ~0ull;
-  uint64_t idle_since = 0;
+  unsigned in_take = 0, in_done = 0, out_tail = 0;
+  unsigned long long n_upd = 0, n_hops = 0, n_fail = 0;
   double esum = 0.0;
   unsigned backoff = 32;
   bool failed = false;
-  // tk0: processed this iteration (rows in wb), tk1: its W stage is due, tk2: its R stage
-  // is due.  sl*: their slots; slf: the free slot the next popped token takes.
-  int tk0 = -1, tk1 = -1, tk2 = -1;
-  int sl0 = 0, sl1 = 1, sl2 = 2, slf = 3;
-  Raw wb[kPF][NV];
-#pragma unroll
-  for (int i = 0; i < kPF; ++i)
-#pragma unroll
-    for (int q = 0; q < NV; ++q) wb[i][q] = nd::zero_raw<Raw>();
+  // tk0: processed this iteration, in inbox slot in_done % kInbox; the token taken ahead
+  // of it (its first rows prefetched, its indices copied) is processed next iteration
+  int tk0 = -1;
 
   while (true) {
-    cp_async_wait<0>();  // the previous iteration's copies ...
-    __syncwarp();        // ... visible to every lane
-    // ---- a priority token at this block: every live warp joins the visit -------------
+    {
+      int stop = 0;
+      if (lane == 0) stop = ld_volatile_shared(&hdr->stop);
+      if (__shfl_sync(kFull, stop, 0)) break;
+    }
+    // ---- a priority token at this block: every live compute warp joins the visit -------
     if (a.cta_heavy) {
       int hv = -1;
-      if (lane == 0) hv = ld_volatile_shared(&hdr->hv_tok);
+      if (lane == 0) {
+        hv = ld_volatile_shared(&hdr->hv_tok);
+        if (hv >= 0) hv = static_cast<int>(ld_acquire_cta_u32(reinterpret_cast<const unsigned*>(&hdr->hv_tok)));
+      }
       hv = __shfl_sync(kFull, hv, 0);
       if (hv >= 0) {
+        cp_async_wait<0>();  // tk0's indices land before the region is reused
+        __syncwarp();
         if (!cta_join(join_bar, join_phase, a, lane)) break;
-        if (leader && lane == 0) st_volatile_shared(&hdr->hv_tok, -1);  // every warp has read it
+        if (leader && lane == 0) st_release_cta_u32(reinterpret_cast<unsigned*>(&hdr->hv_tok), 0xffffffffu);
         CtaVisitOut vo{0.f, 0};
-        cta_visit<Store, NV>(hv, a, s, C, nw_live, wib, lane, vo);
+        cta_visit<Store, NV>(hv, a, s, C, nc_live, wib, lane, vo);
         if (leader) {
-          hv_held = false;
-          const int4 ma = __ldcg(a.mailbox + 2 * static_cast<int64_t>(hv));
-          const int4 mb = __ldcg(a.mailbox + 2 * static_cast<int64_t>(hv) + 1);
+          const int4 ma = __ldcg(a.mailbox + 4 * static_cast<int64_t>(hv));
+          const int4 mb = __ldcg(a.mailbox + 4 * static_cast<int64_t>(hv) + 1);
           int npos = ma.w + 1, nep = mb.x;
           if (npos == (mb.y & 0x7fffffff)) {
             npos = 0;
@@ -972,48 +1222,76 @@ __global__ void __launch_bounds__(256, 2) nomad_async2_kernel(nomad::AsyncArgs a
           const bool retire = nep >= a.target_epoch;
           n_upd += static_cast<unsigned long long>(vo.len);
           ++n_hops;
+          int ok = 1;
           if (lane == 0) {
-            int4 nx = make_int4(0, 0, 0, 0);
+            unsigned qr = 1u;
             if (!retire) {
-              nx = __ldg(a.segs + lo_hi(mb.z, mb.w) + npos);
-              int4* mbox = a.mailbox + 2 * static_cast<int64_t>(hv);
+              const int4 nx = __ldg(a.segs + lo_hi(mb.z, mb.w) + npos);
+              int4* mbox = a.mailbox + 4 * static_cast<int64_t>(hv);
               __stcg(mbox, make_int4(nx.x, nx.y, nx.z, npos));
               __stcg(mbox + 1, make_int4(nep, mb.y, mb.z, mb.w));
+              qr = static_cast<unsigned>(P + nx.w) << 1;
             }
             esum += static_cast<double>(vo.e2);
-            ++pending;
-            fence_acq_rel_gpu();  // the column (stored by the last warp before the exit barrier) and mailbox
-            if (retire) {
-              if (a.finish_ns) a.finish_ns[hv] = nd::globaltimer();
-              atomicAdd(&a.ctrl[0], 1);
-            } else {
-              const int q = P + nx.w;
-              const unsigned seq = atomicAdd(&a.tails[q], 1u);
-              st_relaxed_u64(a.ring_hi + static_cast<int64_t>(nx.w) * (a.mask_hi + 1) + (seq & a.mask_hi),
-                             (static_cast<unsigned long long>(seq) << 32) | static_cast<unsigned>(hv));
-            }
+            // the column (stored by the last warp before the visit's exit barrier) and the
+            // mailbox precede the outbox entry
+            ok = outbox_put(B, out_tail, hv, qr, hdr, a);
           }
-          __syncwarp();
-        }
-        // the visit may have changed rows that tk0's prefetched registers hold
-        if (tk0 >= 0) {
-          const SlotHdr* hd = reinterpret_cast<const SlotHdr*>(slots + static_cast<size_t>(sl0) * s.slot_bytes);
-          const int len = hd->a.z;
-          if (len < s.heavy_min) {
-#pragma unroll
-            for (int i = 0; i < kPF; ++i)
-              if (i < len) load_row_regs<Store, NV>(W, hd->rv[i].x, s, lane, wb[i]);
-          }
+          if (!__shfl_sync(kFull, ok, 0)) break;
         }
       }
     }
-    // ---- process tk0 ----------------------------------------------------------------
-    int push_q = -1;
-    unsigned push_seq = 0;
-    if (tk0 >= 0) {
-      char* slot = slots + static_cast<size_t>(sl0) * s.slot_bytes;
+    // ---- take the next token ahead of processing tk0: its mailbox and column have
+    //      (usually) landed; prefetch its first rows into L1 and copy its indices -------
+    int newtok = -1;
+    if (lane == 0) {
+      const unsigned long long e = ld_acquire_cta_u64(&B.inbox[in_take % kInbox]);
+      if (static_cast<unsigned>(e >> 32) == in_take) {
+        const uint32_t bar = smem_u32(&B.bars[in_take % kInbox]);
+        const uint32_t par = (in_take / kInbox) & 1u;
+        uint64_t t0 = 0;
+        bool ok = true;
+        for (uint32_t it = 0; !mbar_try_wait(bar, par); ++it) {
+          if ((it & 63u) == 0) {
+            const uint64_t now = nd::globaltimer();
+            if (it == 0) {
+              t0 = now;
+            } else if (static_cast<int64_t>(now - t0) > a.budget_ns) {
+              atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
+              ok = false;
+              break;
+            }
+          }
+        }
+        newtok = ok ? static_cast<int>(e & 0x7fffffffull) : -2;
+        if (ok) ++in_take;
+      }
+    }
+    newtok = __shfl_sync(kFull, newtok, 0);
+    if (newtok == -2) {
+      failed = true;
+      break;
+    }
+    __syncwarp();
+    const bool took = newtok >= 0;
+    if (took) {
+      char* slot = slots + static_cast<size_t>((in_done + (tk0 >= 0 ? 1u : 0u)) % kInbox) * s.slot_bytes;
       const SlotHdr* hd = reinterpret_cast<const SlotHdr*>(slot);
-      const int4 ma = hd->a, mb = hd->b, nx = hd->nxt;
+      const int len = hd->a.z;
+      if (len < s.heavy_min && lane < 5 * min(len, kPF)) {  // 5 lines cover a row of <= 512 bytes
+        const int line = lane % 5;
+        if (line * 128 < s.row_bytes)
+          prefetch_l1(static_cast<const char*>(W) + static_cast<int64_t>(first_rating(hd, lane / 5).x) * s.row_bytes +
+                      line * 128);
+      }
+      stage_r(slot, a, s.heavy_min, lane);
+      cp_async_commit();
+    }
+    // ---- process tk0 ----------------------------------------------------------------
+    if (tk0 >= 0) {
+      char* slot = slots + static_cast<size_t>(in_done % kInbox) * s.slot_bytes;
+      const SlotHdr* hd = reinterpret_cast<const SlotHdr*>(slot);
+      const int4 ma = hd->a, mb = hd->b;
       const int len = ma.z, pos = ma.w, ep = mb.x;
       const int nseg = mb.y & 0x7fffffff;
       const float step = __ldg(&a.steps[min(ep, a.n_steps - 1)]);
@@ -1026,14 +1304,18 @@ __global__ void __launch_bounds__(256, 2) nomad_async2_kernel(nomad::AsyncArgs a
         const int v = lane + 32 * q;
         nd::unpack(v < s.nvec ? hs[v] : nd::zero_raw<Raw>(), h[q]);
       }
+      // tk0's copies (indices, next visit) are the older group when a token was just taken
+      if (took) cp_async_wait<1>(); else cp_async_wait<0>();
+      __syncwarp();
       float e2;
       if (len >= s.heavy_min)
         e2 = visit_long<Store, NV>(hd, lo_hi(ma.x, ma.y), len, h, W, s, R, a.ratings, step, a.lambda, colkey, lane,
                                    a.ctrl, a.budget_ns, failed);
       else
-        e2 = visit_short<Store, NV>(hd, len, wb, h, W, s, step, a.lambda, colkey, lane);
+        e2 = visit_short<Store, NV>(hd, len, h, W, s, step, a.lambda, colkey, lane);
       if (failed) break;
-      // the column goes back to HBM; the mailbox gets the route's next visit
+      // the column goes back to HBM; the mailbox gets the route's next visit, whose first
+      // rows (and indices, for a longer visit) are prefetched into L2 for its worker
       Store* hrow = reinterpret_cast<Store*>(static_cast<char*>(a.f.H) + static_cast<int64_t>(tk0) * s.row_bytes);
       const uint32_t hkey = nd::hash32(colkey ^ static_cast<uint32_t>(pos) * 0x27D4EB2Fu);
 #pragma unroll
@@ -1047,109 +1329,44 @@ __global__ void __launch_bounds__(256, 2) nomad_async2_kernel(nomad::AsyncArgs a
         nep = ep + 1;
       }
       const bool retire = nep >= a.target_epoch;
+      const int4 nx = hd->nxt[0];
       n_upd += static_cast<unsigned long long>(len);
       ++n_hops;
+      if (!retire) {
+        if (lane < 4) {
+          int4 m;
+          if (lane == 0) m = make_int4(nx.x, nx.y, nx.z, npos);
+          else if (lane == 1) m = make_int4(nep, mb.y, mb.z, mb.w);
+          else m = hd->nxt[lane - 1];
+          __stcg(a.mailbox + 4 * static_cast<int64_t>(tk0) + lane, m);
+        } else if (lane < 8 && lane - 4 < min(nx.z, kPF)) {
+          const int r = lane - 4;
+          const int4 q = hd->nxt[1 + (r >> 1)];
+          prefetch_l2(static_cast<const char*>(W) + static_cast<int64_t>((r & 1) ? q.z : q.x) * s.row_bytes,
+                      static_cast<uint32_t>(s.row_bytes));
+        } else if (lane == 8 && nx.z > kPF) {
+          const int64_t st0 = lo_hi(nx.x, nx.y) & ~static_cast<int64_t>(1);  // 16-byte aligned start
+          const int64_t end = lo_hi(nx.x, nx.y) + min(nx.z, kChunk);
+          prefetch_l2(a.ratings + st0, static_cast<uint32_t>(((end - st0) * 8 + 15) & ~15ll));
+        }
+      }
+      if (lane == 0) esum += static_cast<double>(e2);
+      __syncwarp();  // every lane's stores and slot reads precede lane 0's releases
+      int ok = 1;
       if (lane == 0) {
-        if (!retire) {
-          int4* mbox = a.mailbox + 2 * static_cast<int64_t>(tk0);
-          __stcg(mbox, make_int4(nx.x, nx.y, nx.z, npos));
-          __stcg(mbox + 1, make_int4(nep, mb.y, mb.z, mb.w));
-        }
-        esum += static_cast<double>(e2);
-        ++pending;
+        ok = outbox_put(B, out_tail, tk0, retire ? 1u : static_cast<unsigned>(nx.w) << 1, hdr, a);
+        st_release_cta_u32(&B.in_head, in_done + 1);  // the slot goes back to the pop warp
       }
-      __syncwarp();  // every lane's stores precede lane 0's release fence
-      if (lane == 0) {
-        fence_acq_rel_gpu();
-        if (retire) {
-          if (a.finish_ns) a.finish_ns[tk0] = nd::globaltimer();
-          atomicAdd(&a.ctrl[0], 1);
-        } else {
-          push_q = nx.w;
-          push_seq = atomicAdd(&a.tails[push_q], 1u);  // the entry store follows the copies below
-        }
-        if (pending >= 64) {
-          atomicAdd(a.progress, pending);
-          pending = 0;
-        }
-      }
+      ++in_done;  // warp-uniform: every lane locates slots by it
+      if (!__shfl_sync(kFull, ok, 0)) break;
     }
-    // ---- W stage for tk1: its first rows (after this visit's row stores) ---------------
-    if (tk1 >= 0) {
-      const SlotHdr* hd = reinterpret_cast<const SlotHdr*>(slots + static_cast<size_t>(sl1) * s.slot_bytes);
-      const int len = hd->a.z;
-      if (len < s.heavy_min) {
-#pragma unroll
-        for (int i = 0; i < kPF; ++i)
-          if (i < len) load_row_regs<Store, NV>(W, hd->rv[i].x, s, lane, wb[i]);
-      }
-    }
-    // ---- R stage for tk2 ---------------------------------------------------------------
-    if (tk2 >= 0) stage_r(slots + static_cast<size_t>(sl2) * s.slot_bytes, a, lane);
-    // ---- D stage for a newly taken token (priority ring first) ---------------------------
-    int newtok = -1;
-    if (lane == 0) {
-      if (leader && !hv_held && entry_valid(probe_hi, head_hi)) {  // every warp sees it next iteration
-        st_volatile_shared(&hdr->hv_tok, static_cast<int>(probe_hi & 0x7fffffffull));
-        hv_held = true;
-        ++head_hi;
-      }
-      if (entry_valid(probe_lo, head_lo)) {
-        newtok = static_cast<int>(probe_lo & 0x7fffffffull);
-        ++head_lo;
-      }
-    }
-    newtok = __shfl_sync(kFull, newtok, 0);
-    if (newtok >= 0) stage_d(slots + static_cast<size_t>(slf) * s.slot_bytes, newtok, a, s.row_bytes, lane);
-    cp_async_commit();
-    if (lane == 0) {
-      if (leader) probe_hi = ld_acquire_u64(my_hi + (head_hi & a.mask_hi));  // for the next iteration
-      probe_lo = ld_acquire_u64(my_lo + (head_lo & a.mask_lo));
-      if (push_q >= 0)  // publish the processed token
-        st_relaxed_u64(a.ring_lo + static_cast<int64_t>(push_q) * (a.mask_lo + 1) + (push_seq & a.mask_lo),
-                       (static_cast<unsigned long long>(push_seq) << 32) | static_cast<unsigned>(tk0));
-    }
-    // ---- shift the pipeline; the processed token's slot becomes the free one -----------
-    const int freed = sl0;
-    tk0 = tk1;
-    sl0 = sl1;
-    tk1 = tk2;
-    sl1 = sl2;
-    tk2 = newtok;
-    sl2 = slf;
-    slf = freed;
-    if (tk0 < 0 && tk1 < 0 && tk2 < 0) {
-      // nothing in the pipeline: idle poll
-      int stop = 0;
-      if (lane == 0 && (++n_fail & 7) == 1) {
-        if (pending) {
-          atomicAdd(a.progress, pending);
-          pending = 0;
-        }
-        if (nd::ld_acquire(&a.ctrl[1]) != 0 || nd::ld_acquire(&a.ctrl[0]) >= a.n_active) {
-          stop = 1;
-        } else {
-          const unsigned long long pr = nd::ld_relaxed_u64(a.progress);
-          const uint64_t now = nd::globaltimer();
-          if (pr != seen) {
-            seen = pr;
-            idle_since = now;
-          } else if (static_cast<int64_t>(now - idle_since) > a.budget_ns) {
-            atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
-            stop = 1;
-          }
-        }
-      }
-      if (__shfl_sync(kFull, stop, 0)) break;
+    tk0 = newtok;
+    if (tk0 < 0) {
+      ++n_fail;
       __nanosleep(backoff);
       backoff = min(backoff * 2, 256u);
     } else {
       backoff = 32;
-      if ((n_hops & 15) == 0) {
-        int stop = 0;
-        if (lane == 0) stop = nd::ld_acquire(&a.ctrl[1]) != 0;
-        if (__shfl_sync(kFull, stop, 0)) break;
-      }
     }
   }
   cp_async_wait<0>();
@@ -1160,10 +1377,8 @@ __global__ void __launch_bounds__(256, 2) nomad_async2_kernel(nomad::AsyncArgs a
       }
     }
   }
+  if (failed && lane == 0) st_volatile_shared(&hdr->stop, 1);
   if (lane == 0) {
-    a.heads[w] = head_lo;
-    if (leader) a.heads[P + blockIdx.x] = head_hi;
-    if (pending) atomicAdd(a.progress, pending);
     atomicAdd(&a.stats[0], n_upd);
     atomicAdd(&a.stats[1], n_hops);
     atomicAdd(&a.stats[2], n_fail);
@@ -1171,8 +1386,9 @@ __global__ void __launch_bounds__(256, 2) nomad_async2_kernel(nomad::AsyncArgs a
   }
 }
 
-// Per launch: every active token's mailbox gets its first visit (pass count `ep`), and
-// the token enters its first queue at sequence tails[q] + rank (column order in a queue).
+// Per launch: every active token's mailbox gets its first visit (pass count `ep`) with the
+// visit's first ratings, and the token enters its first queue at sequence tails[q] + rank
+// (column order in a queue).
 __global__ void seed_queues_kernel(nomad::AsyncArgs a, const int4* __restrict__ first_mail,
                                    const int2* __restrict__ first_q, int n, int ep) {
   const int P = a.P;
@@ -1181,8 +1397,12 @@ __global__ void seed_queues_kernel(nomad::AsyncArgs a, const int4* __restrict__ 
     if (fq.x < 0) continue;
     int4 m1 = first_mail[2 * j + 1];
     m1.x = ep;
-    a.mailbox[2 * static_cast<int64_t>(j)] = first_mail[2 * j];
-    a.mailbox[2 * static_cast<int64_t>(j) + 1] = m1;
+    const int64_t vb = lo_hi(m1.z, m1.w);
+    int4* mb = a.mailbox + 4 * static_cast<int64_t>(j);
+    mb[0] = first_mail[2 * j];
+    mb[1] = m1;
+    mb[2] = a.segx[3 * vb + 1];
+    mb[3] = a.segx[3 * vb + 2];
     const unsigned seq = a.tails[fq.x] + static_cast<unsigned>(fq.y);
     unsigned long long* rq = fq.x >= P ? a.ring_hi + static_cast<int64_t>(fq.x - P) * (a.mask_hi + 1) + (seq & a.mask_hi)
                                        : a.ring_lo + static_cast<int64_t>(fq.x) * (a.mask_lo + 1) + (seq & a.mask_lo);
@@ -1197,16 +1417,31 @@ __global__ void advance_tails_kernel(unsigned* tails, const int* __restrict__ co
 __global__ void drain_queues_kernel(unsigned* heads, const unsigned* tails, int nq) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) heads[q] = tails[q];
 }
+// Extended visit table: each visit {start, len, worker} followed by its first four ratings.
+__global__ void build_segx_kernel(const int4* __restrict__ segs, const int2* __restrict__ ratings, int64_t nseg,
+                                  int4* __restrict__ segx) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nseg;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int4 sg = segs[i];
+    const int64_t start = lo_hi(sg.x, sg.y);
+    int2 r[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r[k] = k < sg.z ? ratings[start + k] : make_int2(0, 0);
+    segx[3 * i] = sg;
+    segx[3 * i + 1] = make_int4(r[0].x, r[0].y, r[1].x, r[1].y);
+    segx[3 * i + 2] = make_int4(r[2].x, r[2].y, r[3].x, r[3].y);
+  }
+}
 
 template <typename Store, int NV>
-size_t smem_per_block(int warps, int kpad, int cta_heavy) {
+size_t smem_per_block(int ncw, int kpad, int cta_heavy) {
   const size_t row_bytes = static_cast<size_t>(kpad) * sizeof(Store);
   const size_t slot = sizeof(SlotHdr) + row_bytes;
-  size_t region = static_cast<size_t>(warps) * kRing * kBlk * row_bytes;
+  size_t region = static_cast<size_t>(ncw) * kRing * kBlk * row_bytes;
   if (cta_heavy) region = std::max(region, cta_region_bytes(kpad, static_cast<int>(sizeof(Store))));
   static_assert(sizeof(SlotHdr) % 16 == 0 && kBarBytes % 16 == 0, "16-byte alignment of the per-warp layout");
   // every term is a multiple of 16 (row_bytes is)
-  return kCtaHdrBytes + static_cast<size_t>(warps) * (kStages * slot + kBarBytes + 128) + region;
+  return kCtaHdrBytes + static_cast<size_t>(ncw) * (sizeof(WarpBox) + kInbox * slot + kBarBytes + 128) + region;
 }
 
 template <typename Store, int NV>
@@ -1217,16 +1452,24 @@ cudaError_t launch2_t(const nomad::AsyncArgs& a, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<nomad::AsyncArgs*>(&a)};
   return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(&nomad_async2_kernel<Store, NV>), dim3(a.grid),
-                                     dim3(a.warps_per_block * 32), args, smem, st);
+                                     dim3((a.warps_per_block + 2) * 32), args, smem, st);
 }
 
 template <typename Store, int NV>
-cudaError_t occ2_t(int warps, int kpad, int cta_heavy, int* bps) {
-  const size_t smem = smem_per_block<Store, NV>(warps, kpad, cta_heavy);
-  cudaError_t e = cudaFuncSetAttribute(&nomad_async2_kernel<Store, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+cudaError_t occ2_t(int ncw, int kpad, int cta_heavy, int* bps) {
+  const size_t smem = smem_per_block<Store, NV>(ncw, kpad, cta_heavy);
+  int dev = 0, max_smem = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if (smem > static_cast<size_t>(max_smem)) {  // does not fit: no block per SM
+    *bps = 0;
+    return cudaSuccess;
+  }
+  e = cudaFuncSetAttribute(&nomad_async2_kernel<Store, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, &nomad_async2_kernel<Store, NV>, warps * 32, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, &nomad_async2_kernel<Store, NV>, (ncw + 2) * 32, smem);
 }
 
 }  // namespace
@@ -1249,18 +1492,18 @@ cudaError_t launch_async2(const AsyncArgs& a, cudaStream_t s) {
   }
 }
 
-cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int cta_heavy, int* bps) {
+cudaError_t async2_occupancy(int bf16, int nv, int ncw, int kpad, int cta_heavy, int* bps) {
   if (bf16) {
     switch (nv) {
-      case 1: return occ2_t<__nv_bfloat16, 1>(warps, kpad, cta_heavy, bps);
-      case 2: return occ2_t<__nv_bfloat16, 2>(warps, kpad, cta_heavy, bps);
-      default: return occ2_t<__nv_bfloat16, 4>(warps, kpad, cta_heavy, bps);
+      case 1: return occ2_t<__nv_bfloat16, 1>(ncw, kpad, cta_heavy, bps);
+      case 2: return occ2_t<__nv_bfloat16, 2>(ncw, kpad, cta_heavy, bps);
+      default: return occ2_t<__nv_bfloat16, 4>(ncw, kpad, cta_heavy, bps);
     }
   }
   switch (nv) {
-    case 1: return occ2_t<float, 1>(warps, kpad, cta_heavy, bps);
-    case 2: return occ2_t<float, 2>(warps, kpad, cta_heavy, bps);
-    default: return occ2_t<float, 4>(warps, kpad, cta_heavy, bps);
+    case 1: return occ2_t<float, 1>(ncw, kpad, cta_heavy, bps);
+    case 2: return occ2_t<float, 2>(ncw, kpad, cta_heavy, bps);
+    default: return occ2_t<float, 4>(ncw, kpad, cta_heavy, bps);
   }
 }
 
@@ -1280,6 +1523,13 @@ cudaError_t launch_seed_queues(const AsyncArgs& a, const int4* first_mail, const
 
 cudaError_t launch_drain_queues(const AsyncArgs& a, cudaStream_t s) {
   drain_queues_kernel<<<(2 * a.P + 255) / 256, 256, 0, s>>>(a.heads, a.tails, 2 * a.P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_segx(const int4* segs, const int2* ratings, int64_t nseg, int4* segx, cudaStream_t s) {
+  if (nseg <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((nseg + 255) / 256, 1 << 16);
+  build_segx_kernel<<<static_cast<int>(blocks), 256, 0, s>>>(segs, ratings, nseg, segx);
   return cudaGetLastError();
 }
 

@@ -38,7 +38,7 @@ struct AsyncArgs {
   uint32_t seed32 = 0;
   int64_t budget_ns = 0;
   int32_t exact = 0;
-  int32_t warps_per_block = 0, grid = 0;
+  int32_t warps_per_block = 0, grid = 0;  // pipelined kernel: compute warps (workers) per block
   int32_t heavy_min = 14;  // visits with at least this many ratings take the blocked path
   unsigned long long* finish_ns = nullptr;  // [n] globaltimer when each token retired
   // ring queues of the pipelined kernel: worker w's ring is ring_lo[w*(mask_lo+1)..];
@@ -49,7 +49,8 @@ struct AsyncArgs {
   unsigned mask_lo = 0, mask_hi = 0;
   unsigned* tails = nullptr;  // [2P] producer counters
   unsigned* heads = nullptr;  // [2P] consumer counters
-  int4* mailbox = nullptr;    // [2n] next visit of each token (two int4)
+  int4* mailbox = nullptr;    // [4n] next visit of each token (four int4)
+  const int4* segx = nullptr; // [3 * segments] each visit followed by its first four ratings
   int32_t cta_heavy = 0;      // priority tokens visit thread blocks, whose warps process them together
 };
 
@@ -94,6 +95,7 @@ cudaError_t launch_async2(const AsyncArgs& a, cudaStream_t s);
 cudaError_t launch_seed_queues(const AsyncArgs& a, const int4* first_mail, const int2* first_q,
                                const int* counts, int n, int ep, cudaStream_t s);
 cudaError_t launch_drain_queues(const AsyncArgs& a, cudaStream_t s);
+cudaError_t launch_build_segx(const int4* segs, const int2* ratings, int64_t nseg, int4* segx, cudaStream_t s);
 cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int cta_heavy, int* blocks_per_sm);
 cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);

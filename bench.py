@@ -7,7 +7,9 @@ planted rank-20 model), k = 100, lrate 0.002, drate 0.05, reg 0.05: seeded synth
 data with the shape of the Netflix-prize matrix (the dataset itself is not used).
 
 One step = one epoch of the async NOMAD kernel: every training rating updated once,
-column tokens passed between 4,864 worker warps through device queues.  Both storage
+column tokens passed between worker warps (14 per thread block, one block per SM: 2,128
+workers) through device ring queues; columns long enough to set the epoch time visit
+whole thread blocks.  Both storage
 forms run (fp32 and bf16 with stochastic rounding); the headline value is the bf16
 form.  The device-resident number (`value`) sums CUDA-event time of the K timed epoch
 launches; `e2e` times the whole job through the C-ABI from host buffers (init with the
@@ -57,6 +59,11 @@ def parse():
     ap.add_argument("--workers", type=int, default=0)
     ap.add_argument("--wpb", type=int, default=0)
     ap.add_argument("--bps", type=int, default=0)
+    ap.add_argument("--forms", default="fp32,bf16",
+                    help="storage forms to run (the headline is bf16; profiling runs pick one)")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="shrink rows, columns and ratings by this factor (profiling captures "
+                         "of a smaller case of the same shape; not a headline number)")
     return ap.parse_args()
 
 
@@ -291,20 +298,30 @@ def main_ours(args, dist):
         raise SystemExit(f"cuda:{device} is not an sm_103 device")
     K, W = args.steps, args.warmup
     t = time.perf_counter()
-    train, test = ng.synth(WORKLOAD_ID)
+    if args.scale == 1.0:
+        train, test = ng.synth(WORKLOAD_ID)
+    else:
+        s = args.scale
+        train, test = ng.synth(ng.synth_spec(WORKLOAD_ID, m=int(480189 * s), n=int(17770 * s),
+                                             nnz_train=int(100480507 * s), nnz_test=int(1408395 * s)))
     log(f"[bench] workload generated in {time.perf_counter() - t:.1f} s "
         f"(nnz {train.nnz} / {test.nnz})")
     clocks = Clocks(device)
     dist.barrier()
     res = {}
-    for form in ("fp32", "bf16"):
+    forms = [f for f in ("fp32", "bf16") if f in args.forms.split(",")]
+    for form in forms:
         res[form] = run_form(ng, train, test, form, W, K, device, args,
-                             clocks if form == "bf16" else None)
+                             clocks if form == forms[-1] else None)
         log(f"[bench] {form}: {res[form]['updates_per_s']:.4g} updates/s, "
             f"{res[form]['ms_per_step']:.2f} ms/epoch, test RMSE "
             f"{res[form]['epochs'][-1]['test_rmse']:.5f}, init {res[form]['init_s']:.1f} s")
     clk = clocks.stop()
     dist.barrier()
+    if args.scale != 1.0 or len(forms) < 2:  # a profiling run: no headline line
+        log(json.dumps({f: {"updates_per_s": r["updates_per_s"], "ms_per_step": r["ms_per_step"]}
+                        for f, r in res.items()}))
+        return
     b = res["bf16"]
     # whole-job aggregate over ranks: updates summed, time = slowest rank
     tot_upd = dist.reduce(b["timed_updates"], "sum")
@@ -341,10 +358,11 @@ def main_ours(args, dist):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"of {peak_kind}",
                      "bytes_per_update": BYTES_PER_UPDATE["bf16"],
-                     "kernel": "nomad_async_kernel<bf16> (one launch per epoch)"},
+                     "kernel": "nomad_async2_kernel<bf16> (one launch per epoch)"},
         "clocks": clk,
         "e2e": e2e,
-        "gpu_launches": K,
+        # per timed epoch: the queue seeding kernel, the tail advance and the async kernel
+        "gpu_launches": 3 * K,
         "workers": b["info"]["workers"], "segments_per_epoch": b["info"]["segments"],
         "max_column": b["info"]["max_column"],
         "host_updates_per_s": b["host_updates_per_s"],

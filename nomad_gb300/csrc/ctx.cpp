@@ -416,10 +416,11 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.exact = c->prm.exact;
   a.warps_per_block = c->wpb;
   a.grid = c->grid;
-  // Seeding reads the ring geometry (a.P) and must follow every assignment above.
+  // Seeding reads the ring geometry (a.P) and must follow every assignment above; it is
+  // part of the timed epoch.
+  CK(cudaEventRecord(c->ev0, c->stream));
   if (pipelined && !(c->prm.debug_flags & 1))
     CK(nomad::launch_seed_queues(a, c->first_mail, c->first_q, c->q_count, n, c->epochs_done, c->stream));
-  CK(cudaEventRecord(c->ev0, c->stream));
   if (c->n_active > 0) {
     if (c->prm.exact)
       CK(nomad::launch_async(a, c->stream));

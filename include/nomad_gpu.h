@@ -223,6 +223,37 @@ int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t n, int32_t 
                           const int64_t* col_ptr, int64_t nnz, int32_t blocks,
                           double* sse_out, void* stream);
 
+/* ---- batched problems ------------------------------------------------------------ */
+/* Many independent completion problems of uneven m, n, nnz and rank trained together:
+ * one persistent launch per epoch (captured once as a CUDA graph and replayed), fed by a
+ * device work queue of problems sorted by size (largest first); a warp takes a problem
+ * and runs its epoch with the reference's one-worker schedule -- columns in index order,
+ * each column's ratings in row order (nb_main.cpp:82-97, 554-558 with one thread and one
+ * rank).  With params.exact = 1 and FP32 storage every problem's factors equal the
+ * one-worker replay bit for bit; otherwise FMA arithmetic, FP32 or BF16_SR storage.
+ * Uses params.precision, exact, lrate, drate, reg, seed, init_parts, device; dim comes
+ * per problem (at most 128).  No counterpart in the reference (it trains one problem
+ * per run). */
+typedef struct nomad_gpu_batch_problem {
+  int32_t m, n, dim, reserved;
+  nomad_gpu_matrix train, test; /* as in nomad_gpu_problem                             */
+  const float* W0;              /* optional [m x dim]; NULL: reference init            */
+  const float* H0;              /* optional [n x dim]                                  */
+} nomad_gpu_batch_problem;
+
+typedef struct nomad_gpu_batch nomad_gpu_batch; /* opaque */
+
+int nomad_gpu_batch_init(nomad_gpu_batch** out, const nomad_gpu_batch_problem* problems,
+                         int32_t count, const nomad_gpu_params* params);
+/* n_epochs epochs of every problem; st->updates sums over problems, device_ms times the
+ * graph launches (CUDA events). */
+int nomad_gpu_batch_epoch(nomad_gpu_batch* b, int32_t n_epochs, nomad_gpu_epoch_stats* st);
+/* Per-problem RMSE (FP64 sums), arrays of `count` doubles; a problem without ratings in a
+ * set gets 0. */
+int nomad_gpu_batch_rmse(nomad_gpu_batch* b, double* train_rmse, double* test_rmse);
+int nomad_gpu_batch_get_factors(nomad_gpu_batch* b, int32_t problem, float* W, float* H);
+void nomad_gpu_batch_destroy(nomad_gpu_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -113,6 +113,13 @@ typedef struct nomad_synth_spec {
  * Returns NOMAD_ERR_INVALID_ARG for other numbers. */
 int nomad_synth_preset(int32_t workload, nomad_synth_spec* spec);
 
+/* Problem `index` of the batched workload (BASELINE configuration 5), drawn from `seed`:
+ * m log-uniform in [200, 20,000], n log-uniform in [100, 5,000], density log-uniform in
+ * [0.5%, 5%] (90% train / 10% test cells, uniform without replacement), rank k drawn from
+ * {16, 32, 64}, planted rank k/4 with N(0, (k/4)^-1/2) factors, values <w*,h*> + N(0, 0.1^2).
+ * Fills spec (for nomad_synth_generate) and *dim = k. */
+int nomad_synth_batch_problem(uint64_t seed, int32_t index, nomad_synth_spec* spec, int32_t* dim);
+
 /* Generate the train and test matrices of a spec (row-major, columns ascending in
  * each row).  Deterministic for a given spec, whatever the thread count. */
 int nomad_synth_generate(const nomad_synth_spec* spec, nomad_io_matrix* train,

@@ -126,6 +126,16 @@ def synth(workload_or_spec, **overrides):
     return RatingMatrix._from_io(tr), RatingMatrix._from_io(te)
 
 
+def synth_batch_problem(index, seed=12345):
+    """Problem `index` of the batched workload (4,096 problems of uneven shape and rank):
+    (train, test, dim)."""
+    spec, dim = _abi.SynthSpec(), ctypes.c_int32()
+    check(lib().nomad_synth_batch_problem(int(seed), int(index), ctypes.byref(spec),
+                                          ctypes.byref(dim)), "nomad_synth_batch_problem")
+    train, test = synth(spec)
+    return train, test, dim.value
+
+
 def reference_init(m, n, dim, seed=12345, parts=1):
     """The reference's initial factors (float32 W[m,dim], H[n,dim])."""
     W = np.empty((m, dim), np.float32)
@@ -224,6 +234,78 @@ class Nomad:
         if self._ctx:
             lib().nomad_gpu_destroy(self._ctx)
             self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent problems trained together (nomad_gpu_batch): one graph-captured
+    persistent launch per epoch; each problem runs the one-worker schedule.
+
+        problems = [ng.synth_batch_problem(i) for i in range(64)]   # (train, test, dim)
+        with ng.Batch(problems, lrate=0.002, drate=0.1, reg=0.05) as b:
+            b.epoch(30)
+            train_rmse, test_rmse = b.rmse()
+    """
+
+    def __init__(self, problems, params=None, **kw):
+        self._b = ctypes.c_void_p()
+        p = params if params is not None else default_params(**kw)
+        self.params = p
+        self.shapes = []
+        arr = (_abi.BatchProblem * len(problems))()
+        self._keep = []
+        for i, prob in enumerate(problems):
+            train, test, dim = prob[0], prob[1], int(prob[2])
+            W0 = H0 = None
+            if len(prob) > 3 and prob[3] is not None:
+                W0 = np.ascontiguousarray(prob[3], np.float32)
+            if len(prob) > 4 and prob[4] is not None:
+                H0 = np.ascontiguousarray(prob[4], np.float32)
+            self._keep += [train, test, W0, H0]
+            arr[i] = _abi.BatchProblem(train.m, train.n, dim, 0, train._c(), test._c(), _ptr(W0), _ptr(H0))
+            self.shapes.append((train.m, train.n, dim))
+        check(lib().nomad_gpu_batch_init(ctypes.byref(self._b), arr, len(problems), ctypes.byref(p)),
+              "nomad_gpu_batch_init")
+        self._keep = None  # the library copied the host arrays
+
+    @property
+    def count(self):
+        return len(self.shapes)
+
+    def epoch(self, n_epochs=1):
+        st = _abi.EpochStats()
+        check(lib().nomad_gpu_batch_epoch(self._b, n_epochs, ctypes.byref(st)), "nomad_gpu_batch_epoch")
+        return {k: getattr(st, k) for k, _ in _abi.EpochStats._fields_ if k != "reserved0"}
+
+    def rmse(self):
+        tr = np.zeros(self.count, np.float64)
+        te = np.zeros(self.count, np.float64)
+        check(lib().nomad_gpu_batch_rmse(self._b, _ptr(tr), _ptr(te)), "nomad_gpu_batch_rmse")
+        return tr, te
+
+    def factors(self, problem):
+        m, n, dim = self.shapes[problem]
+        W = np.empty((m, dim), np.float32)
+        H = np.empty((n, dim), np.float32)
+        check(lib().nomad_gpu_batch_get_factors(self._b, int(problem), _ptr(W), _ptr(H)),
+              "nomad_gpu_batch_get_factors")
+        return W, H
+
+    def close(self):
+        if self._b:
+            lib().nomad_gpu_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
 
     def __enter__(self):
         return self

@@ -56,6 +56,11 @@ class Problem(ctypes.Structure):
                 ("W0", c_vp), ("H0", c_vp)]
 
 
+class BatchProblem(ctypes.Structure):
+    _fields_ = [("m", c_i32), ("n", c_i32), ("dim", c_i32), ("reserved", c_i32),
+                ("train", Matrix), ("test", Matrix), ("W0", c_vp), ("H0", c_vp)]
+
+
 class EpochStats(ctypes.Structure):
     _fields_ = [("updates", c_i64), ("hops", c_i64), ("failures", c_i64),
                 ("epochs_done", c_i32), ("reserved0", c_i32), ("device_ms", c_dbl),
@@ -107,6 +112,14 @@ SIGNATURES = {
     "nomad_gpu_token_finish_times": (ctypes.c_int, [c_vp, c_vp]),
     "nomad_gpu_sse_noalloc": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,
                                              c_i64, c_i32, c_vp, c_vp]),
+    "nomad_gpu_batch_init": (ctypes.c_int, [ctypes.POINTER(c_vp), ctypes.POINTER(BatchProblem), c_i32,
+                                            ctypes.POINTER(Params)]),
+    "nomad_gpu_batch_epoch": (ctypes.c_int, [c_vp, c_i32, ctypes.POINTER(EpochStats)]),
+    "nomad_gpu_batch_rmse": (ctypes.c_int, [c_vp, c_vp, c_vp]),
+    "nomad_gpu_batch_get_factors": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp]),
+    "nomad_gpu_batch_destroy": (None, [c_vp]),
+    "nomad_synth_batch_problem": (ctypes.c_int, [c_u64, c_i32, ctypes.POINTER(SynthSpec),
+                                                 ctypes.POINTER(c_i32)]),
     "nomad_io_read_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_i32),
                                             ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
                                             ctypes.POINTER(c_i64)]),

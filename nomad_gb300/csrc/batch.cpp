@@ -1,0 +1,355 @@
+// batch.cpp -- the batched-problem C-ABI (include/nomad_gpu.h, nomad_gpu_batch_*): many
+// independent completion problems in one context, trained by one persistent launch per
+// epoch that is captured once as a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "common.h"
+#include "launch.h"
+#include "layout.h"
+
+struct nomad_gpu_batch {
+  nomad_gpu_params prm{};
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<void*> allocs;
+  std::vector<nomad::BatchProblem> probs;
+  nomad::BatchArgs a;
+  int esz = 4;
+  int grid = 0, sse_grid = 0;
+  int32_t n_steps = 0, epochs_done = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+  nomad::set_last_error("%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? NOMAD_ERR_OOM : NOMAD_ERR_CUDA;
+}
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+#define RC(call)         \
+  do {                   \
+    int rc_ = (call);    \
+    if (rc_) return rc_; \
+  } while (0)
+
+template <typename T>
+int dalloc(nomad_gpu_batch* b, T** p, size_t count) {
+  *p = nullptr;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    NOMAD_FAIL(NOMAD_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", std::max<size_t>(count, 1) * sizeof(T),
+               cudaGetErrorString(e));
+  }
+  b->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return NOMAD_OK;
+}
+
+template <typename T>
+int upload(nomad_gpu_batch* b, T** p, const T* src, size_t count) {
+  RC(dalloc(b, p, count));
+  if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, b->stream));
+  return NOMAD_OK;
+}
+
+// Step sizes for every pass count below `needed`.  The captured graph holds the table's
+// address, so a new table means a new graph.
+int ensure_steps(nomad_gpu_batch* b, int32_t needed) {
+  if (needed <= b->n_steps) return NOMAD_OK;
+  int32_t cap = std::max<int32_t>(256, b->n_steps);
+  while (cap < needed) cap *= 2;
+  std::vector<float> h(cap);
+  for (int32_t e = 0; e < cap; ++e) h[e] = nomad::step_size_f32(b->prm.lrate, b->prm.drate, e);
+  float* d = nullptr;
+  RC(upload(b, &d, h.data(), h.size()));
+  CK(cudaStreamSynchronize(b->stream));
+  b->a.steps = d;
+  b->a.n_steps = cap;
+  b->n_steps = cap;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return NOMAD_OK;
+}
+
+// The epoch launch (work-queue kernel + pass-count advance) as a graph.
+int ensure_graph(nomad_gpu_batch* b) {
+  if (b->exec) return NOMAD_OK;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t le = nomad::launch_batch_epoch(b->a, b->grid, b->stream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(le, "nomad::launch_batch_epoch (capture)");
+  }
+  CK(ce);
+  b->graph = g;
+  CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  return NOMAD_OK;
+}
+
+int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t count) {
+  const nomad_gpu_params& p = b->prm;
+  const int threads = nomad::host_threads();
+  CK(cudaSetDevice(b->device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, b->device));
+  if (prop.major * 10 + prop.minor != 103)
+    NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", b->device, prop.major,
+               prop.minor);
+  b->num_sms = prop.multiProcessorCount;
+  CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&b->ev0));
+  CK(cudaEventCreate(&b->ev1));
+  const bool bf16 = p.precision == NOMAD_PREC_BF16_SR;
+  b->esz = bf16 ? 2 : 4;
+
+  // ---- per-problem layout, concatenated ------------------------------------------------
+  b->probs.resize(count);
+  std::vector<nomad::Rating> tr_all, te_all;  // {int32 row, float value}: the device's int2
+  std::vector<int64_t> cp_all, tcp_all;
+  std::vector<int64_t> nnz(count);
+  int64_t w_off = 0, h_off = 0;
+  int64_t max_rows = 0;
+  for (int32_t i = 0; i < count; ++i) {
+    const nomad_gpu_batch_problem& q = P[i];
+    if (q.m <= 0 || q.n <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "problem %d: m and n must be positive", i);
+    if (q.dim <= 0 || q.dim > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "problem %d: dim %d outside [1, 128]", i, q.dim);
+    nomad::Csc tr, te;
+    RC(nomad::build_csc(q.train, q.m, q.n, tr, threads));
+    RC(nomad::build_csc(q.test, q.m, q.n, te, threads));
+    nomad::BatchProblem& pb = b->probs[i];
+    std::memset(&pb, 0, sizeof(pb));
+    pb.m = q.m;
+    pb.n = q.n;
+    pb.dim = q.dim;
+    pb.kpad = bf16 ? (q.dim + 7) / 8 * 8 : (q.dim + 3) / 4 * 4;
+    pb.nvec = pb.kpad / 4;
+    pb.red_width = 1;
+    while (pb.red_width < std::min(pb.nvec, 32)) pb.red_width <<= 1;
+    pb.w_off = w_off;
+    pb.h_off = h_off;
+    w_off += static_cast<int64_t>(q.m) * pb.kpad;
+    h_off += static_cast<int64_t>(q.n) * pb.kpad;
+    max_rows = std::max<int64_t>(max_rows, std::max(q.m, q.n));
+    pb.col_off = static_cast<int64_t>(cp_all.size());
+    pb.test_col_off = static_cast<int64_t>(tcp_all.size());
+    const int64_t tb = static_cast<int64_t>(tr_all.size()), eb = static_cast<int64_t>(te_all.size());
+    for (int64_t c : tr.col_ptr) cp_all.push_back(tb + c);
+    for (int64_t c : te.col_ptr) tcp_all.push_back(eb + c);
+    tr_all.insert(tr_all.end(), tr.ratings.begin(), tr.ratings.end());
+    te_all.insert(te_all.end(), te.ratings.begin(), te.ratings.end());
+    nnz[i] = tr.nnz();
+  }
+  // work queue: the largest problems first, so the longest epochs start first
+  std::vector<int32_t> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return nnz[x] > nnz[y]; });
+
+  nomad::BatchArgs& a = b->a;
+  a.count = count;
+  a.bf16 = bf16;
+  a.exact = p.exact;
+  a.lambda = static_cast<float>(p.reg);
+  a.seed32 = static_cast<uint32_t>(p.seed ^ (p.seed >> 32));
+  char *W = nullptr, *H = nullptr;
+  RC(dalloc(b, &W, static_cast<size_t>(w_off) * b->esz));
+  RC(dalloc(b, &H, static_cast<size_t>(h_off) * b->esz));
+  a.W = W;
+  a.H = H;
+  int2 *tr = nullptr, *te = nullptr;
+  int64_t *cp = nullptr, *tcp = nullptr;
+  nomad::BatchProblem* dp = nullptr;
+  int32_t* dord = nullptr;
+  static_assert(sizeof(nomad::Rating) == sizeof(int2), "rating layout");
+  RC(upload(b, &tr, reinterpret_cast<const int2*>(tr_all.data()), tr_all.size()));
+  RC(upload(b, &te, reinterpret_cast<const int2*>(te_all.data()), te_all.size()));
+  RC(upload(b, &cp, cp_all.data(), cp_all.size()));
+  RC(upload(b, &tcp, tcp_all.data(), tcp_all.size()));
+  RC(upload(b, &dp, b->probs.data(), b->probs.size()));
+  RC(upload(b, &dord, order.data(), order.size()));
+  a.ratings = tr;
+  a.test = te;
+  a.col_ptr = cp;
+  a.test_col_ptr = tcp;
+  a.problems = dp;
+  a.order = dord;
+  RC(dalloc(b, &a.next, 1));
+  RC(dalloc(b, &a.epoch, 1));
+  RC(dalloc(b, &a.stats, 4));
+  RC(dalloc(b, &a.err_sum, 1));
+  RC(dalloc(b, &a.sse, 4 * static_cast<size_t>(count)));
+  CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), b->stream));
+  CK(cudaMemsetAsync(a.epoch, 0, sizeof(int32_t), b->stream));
+
+  // ---- factors: given, or the reference init of each problem, through one staging buffer
+  float* stage = nullptr;
+  RC(dalloc(b, &stage, static_cast<size_t>(max_rows) * 128));
+  std::vector<float> hw;
+  for (int32_t i = 0; i < count; ++i) {
+    const nomad_gpu_batch_problem& q = P[i];
+    const nomad::BatchProblem& pb = b->probs[i];
+    for (int side = 0; side < 2; ++side) {
+      const int64_t rows = side ? q.n : q.m;
+      const float* src = side ? q.H0 : q.W0;
+      if (!src) {
+        hw.assign(static_cast<size_t>(rows) * q.dim, 0.f);
+        RC(nomad_reference_init(side ? 0 : q.m, side ? q.n : 0, q.dim, p.seed, std::max(p.init_parts, 1),
+                                side ? nullptr : hw.data(), side ? hw.data() : nullptr));
+        src = hw.data();
+      }
+      CK(cudaMemcpyAsync(stage, src, static_cast<size_t>(rows) * q.dim * sizeof(float), cudaMemcpyHostToDevice,
+                         b->stream));
+      char* dst = (side ? H : W) + (side ? pb.h_off : pb.w_off) * b->esz;
+      CK(nomad::launch_f32_to_store(stage, dst, rows, q.dim, pb.kpad, bf16, b->stream));
+      CK(cudaStreamSynchronize(b->stream));  // the staging buffer is reused
+    }
+  }
+
+  int bps = 0;
+  CK(nomad::batch_occupancy(bf16, p.exact, &bps));
+  if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
+  b->grid = bps * b->num_sms;
+  b->sse_grid = std::max(1, std::min((count + 3) / 4, 8 * b->num_sms));
+  RC(ensure_steps(b, 64));
+  CK(cudaStreamSynchronize(b->stream));
+  return NOMAD_OK;
+}
+
+void release(nomad_gpu_batch* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (void* q : b->allocs) cudaFree(q);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nomad_gpu_batch_init(nomad_gpu_batch** out, const nomad_gpu_batch_problem* problems, int32_t count,
+                         const nomad_gpu_params* params) {
+  nomad::clear_last_error();
+  if (!out || !problems || !params || count <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid batch arguments");
+  if (params->struct_size != static_cast<int32_t>(sizeof(nomad_gpu_params)))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "params.struct_size mismatch");
+  if (params->precision != NOMAD_PREC_FP32 && params->precision != NOMAD_PREC_BF16_SR)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown precision %d", params->precision);
+  *out = nullptr;
+  nomad_gpu_batch* b = new nomad_gpu_batch();
+  b->prm = *params;
+  b->device = params->device;
+  const int rc = init_impl(b, problems, count);
+  if (rc) {
+    release(b);
+    return rc;
+  }
+  *out = b;
+  return NOMAD_OK;
+}
+
+int nomad_gpu_batch_epoch(nomad_gpu_batch* b, int32_t n_epochs, nomad_gpu_epoch_stats* st) {
+  nomad::clear_last_error();
+  if (!b || n_epochs < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
+  const auto t0 = std::chrono::steady_clock::now();
+  CK(cudaSetDevice(b->device));
+  RC(ensure_steps(b, b->epochs_done + n_epochs + 1));
+  RC(ensure_graph(b));
+  CK(cudaMemsetAsync(b->a.stats, 0, 4 * sizeof(unsigned long long), b->stream));
+  CK(cudaMemsetAsync(b->a.err_sum, 0, sizeof(double), b->stream));
+  CK(cudaEventRecord(b->ev0, b->stream));
+  for (int32_t e = 0; e < n_epochs; ++e) CK(cudaGraphLaunch(b->exec, b->stream));
+  CK(cudaEventRecord(b->ev1, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  unsigned long long stats[4];
+  double esum = 0.0;
+  CK(cudaMemcpy(stats, b->a.stats, sizeof(stats), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&esum, b->a.err_sum, sizeof(double), cudaMemcpyDeviceToHost));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->epochs_done += n_epochs;
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    st->updates = static_cast<int64_t>(stats[0]);
+    st->hops = 0;
+    st->epochs_done = b->epochs_done;
+    st->device_ms = ms;
+    st->online_sse = esum;
+    st->host_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return NOMAD_OK;
+}
+
+int nomad_gpu_batch_rmse(nomad_gpu_batch* b, double* train_rmse, double* test_rmse) {
+  nomad::clear_last_error();
+  if (!b) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null batch");
+  CK(cudaSetDevice(b->device));
+  CK(nomad::launch_batch_sse(b->a, b->sse_grid, b->stream));
+  std::vector<double> s(4 * static_cast<size_t>(b->a.count));
+  CK(cudaMemcpyAsync(s.data(), b->a.sse, s.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  for (int32_t i = 0; i < b->a.count; ++i) {
+    if (train_rmse) train_rmse[i] = s[4 * i + 1] > 0 ? std::sqrt(s[4 * i] / s[4 * i + 1]) : 0.0;
+    if (test_rmse) test_rmse[i] = s[4 * i + 3] > 0 ? std::sqrt(s[4 * i + 2] / s[4 * i + 3]) : 0.0;
+  }
+  return NOMAD_OK;
+}
+
+int nomad_gpu_batch_get_factors(nomad_gpu_batch* b, int32_t problem, float* W, float* H) {
+  nomad::clear_last_error();
+  if (!b || problem < 0 || problem >= b->a.count) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid problem index");
+  CK(cudaSetDevice(b->device));
+  const nomad::BatchProblem& pb = b->probs[problem];
+  for (int side = 0; side < 2; ++side) {
+    float* dst = side ? H : W;
+    if (!dst) continue;
+    const int64_t rows = side ? pb.n : pb.m;
+    float* stage = nullptr;
+    CK(cudaMalloc(&stage, std::max<int64_t>(rows, 1) * pb.dim * sizeof(float)));
+    const char* src = static_cast<const char*>(side ? b->a.H : b->a.W) + (side ? pb.h_off : pb.w_off) * b->esz;
+    cudaError_t e = nomad::launch_store_to_f32(src, stage, rows, pb.dim, pb.kpad, b->a.bf16, b->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dst, stage, static_cast<size_t>(rows) * pb.dim * sizeof(float), cudaMemcpyDeviceToHost,
+                          b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(stage);
+    if (e != cudaSuccess) return cuda_fail(e, "batch factor download");
+  }
+  return NOMAD_OK;
+}
+
+void nomad_gpu_batch_destroy(nomad_gpu_batch* b) {
+  if (b) cudaSetDevice(b->device);
+  release(b);
+}
+
+}  // extern "C"

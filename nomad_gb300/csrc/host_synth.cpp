@@ -206,6 +206,33 @@ int nomad_synth_preset(int32_t workload, nomad_synth_spec* s) {
   return NOMAD_OK;
 }
 
+int nomad_synth_batch_problem(uint64_t seed, int32_t index, nomad_synth_spec* s, int32_t* dim) {
+  nomad::clear_last_error();
+  if (!s || !dim || index < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid batch problem request");
+  std::memset(s, 0, sizeof(*s));
+  s->struct_size = sizeof(*s);
+  s->scale = 1.0;
+  nomad::SplitMix64 rng(nomad::stream_key(seed, 211, static_cast<uint64_t>(index)));
+  auto log_uniform = [&](double lo, double hi) { return lo * std::exp(rng.uniform() * std::log(hi / lo)); };
+  const int32_t m = static_cast<int32_t>(std::lround(log_uniform(200.0, 20000.0)));
+  const int32_t n = static_cast<int32_t>(std::lround(log_uniform(100.0, 5000.0)));
+  const double density = log_uniform(0.005, 0.05);
+  static const int32_t kRanks[3] = {16, 32, 64};
+  const int32_t k = kRanks[rng.below(3)];
+  const int64_t cells = std::max<int64_t>(2, std::llround(density * static_cast<double>(m) * n));
+  s->m = m;
+  s->n = n;
+  s->positions = NOMAD_SYNTH_UNIFORM;
+  s->nnz_test = std::max<int64_t>(1, cells / 10);
+  s->nnz_train = cells - s->nnz_test;
+  s->rank = k / 4;
+  s->factor_std = 1.0 / std::sqrt(static_cast<double>(k / 4));
+  s->noise_std = 0.1;
+  s->seed = nomad::stream_key(seed, 223, static_cast<uint64_t>(index));
+  *dim = k;
+  return NOMAD_OK;
+}
+
 int nomad_synth_generate(const nomad_synth_spec* spec, nomad_io_matrix* train,
                          nomad_io_matrix* test) {
   nomad::clear_last_error();

@@ -444,6 +444,114 @@ cudaError_t occ_t(int warps_per_block, int kpad, int* bps) {
 
 constexpr int kPF = 4;
 
+
+// ---------------------------------------------------------------------------------
+// Batched problems: independent completion problems taken one at a time by a warp from
+// a device work queue (problems by decreasing rating count).  Each problem runs the
+// reference's one-worker schedule -- columns in index order, every column's ratings in
+// row order (nb_main.cpp:82-97, 554-558 with one thread and one rank) -- so the exact
+// form reproduces the one-worker replay of every problem bit for bit.  k <= 128 (one
+// vector of 4 values per lane); lanes past k/4 idle, reductions span the k/4 lanes.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ nomad::DevFactors batch_factors(const nomad::BatchArgs& a, const nomad::BatchProblem& pb,
+                                                           int esz) {
+  nomad::DevFactors f;
+  f.W = static_cast<char*>(a.W) + pb.w_off * esz;
+  f.H = static_cast<char*>(a.H) + pb.h_off * esz;
+  f.m = pb.m;
+  f.n = pb.n;
+  f.dim = pb.dim;
+  f.kpad = pb.kpad;
+  f.nvec = pb.nvec;
+  f.red_width = pb.red_width;
+  f.bf16 = esz == 2;
+  return f;
+}
+
+template <typename Store, bool EXACT>
+__global__ void __launch_bounds__(nomad::kBatchThreads) nomad_batch_kernel(nomad::BatchArgs a) {
+  constexpr int NV = 1;
+  constexpr int E = Vec<Store>::E;
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31;
+  float* xbuf = smem + (threadIdx.x >> 5) * 128;  // exact form: one row of products
+  const int ep = *a.epoch;
+  const float step = a.steps[min(ep, a.n_steps - 1)];
+  double esum = 0.0;
+  unsigned long long n_upd = 0;
+  while (true) {
+    int p = 0;
+    if (lane == 0) p = atomicAdd(a.next, 1);
+    p = __shfl_sync(kFull, p, 0);
+    if (p >= a.count) break;
+    const int prob = a.order[p];
+    const nomad::BatchProblem pb = a.problems[prob];
+    const nomad::DevFactors f = batch_factors(a, pb, static_cast<int>(sizeof(Store)));
+    Store* __restrict__ W = static_cast<Store*>(f.W);
+    Store* __restrict__ H = static_cast<Store*>(f.H);
+    const int64_t* cp = a.col_ptr + pb.col_off;
+    const uint32_t pkey = nd::hash32(a.seed32 ^ static_cast<uint32_t>(prob) * 0x27D4EB2Fu);
+    for (int j = 0; j < pb.n; ++j) {
+      const int64_t b = cp[j], e = cp[j + 1];
+      if (b == e) continue;
+      const uint32_t colkey = nd::hash32(pkey ^ static_cast<uint32_t>(j) * 0x85EBCA77u ^
+                                         static_cast<uint32_t>(ep) * 0xC2B2AE3Du);
+      float h[NV][E];
+      load_col<Store, NV>(H, j, f, lane, h);
+      esum += visit_segment<Store, NV, EXACT, 2>(W, f, h, a.ratings, b, static_cast<int>(e - b), step, a.lambda,
+                                                 colkey, lane, xbuf);
+      store_col<Store, NV>(H, j, f, lane, h, nd::hash32(colkey));
+      n_upd += static_cast<unsigned long long>(e - b);
+      __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    atomicAdd(&a.stats[0], n_upd);
+    atomicAdd(a.err_sum, esum);
+  }
+}
+
+// After an epoch launch: the next pass count, and the work queue back at its head.
+__global__ void batch_advance_kernel(int32_t* epoch, int32_t* next) {
+  *epoch += 1;
+  *next = 0;
+}
+
+// Per-problem FP64 squared errors of the train and the test ratings, a warp per problem.
+template <typename Store>
+__global__ void __launch_bounds__(nomad::kBatchThreads) batch_sse_kernel(nomad::BatchArgs a) {
+  constexpr int NV = 1;
+  constexpr int E = Vec<Store>::E;
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int prob = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); prob < a.count; prob += warps) {
+    const nomad::BatchProblem pb = a.problems[prob];
+    const nomad::DevFactors f = batch_factors(a, pb, static_cast<int>(sizeof(Store)));
+    const Store* __restrict__ W = static_cast<const Store*>(f.W);
+    const Store* __restrict__ H = static_cast<const Store*>(f.H);
+    for (int set = 0; set < 2; ++set) {
+      const int2* rt = set ? a.test : a.ratings;
+      const int64_t* cp = set ? a.test_col_ptr + pb.test_col_off : a.col_ptr + pb.col_off;
+      double acc = 0.0;
+      for (int j = 0; j < pb.n; ++j) {
+        float h[NV][E];
+        load_col<Store, NV>(H, j, f, lane, h);
+        for (int64_t o = cp[j]; o < cp[j + 1]; ++o) {
+          const int2 r = __ldg(&rt[o]);
+          float w[NV][E];
+          load_row<Store, NV>(W, r.x, f.kpad, f.nvec, lane, w);
+          const float err = rating_error<Store, NV, false>(h, w, __int_as_float(r.y), f.nvec, f.red_width, f.dim,
+                                                           lane, nullptr);
+          acc += static_cast<double>(err) * err;
+        }
+      }
+      if (lane == 0) {
+        a.sse[4 * static_cast<int64_t>(prob) + 2 * set] = acc;
+        a.sse[4 * static_cast<int64_t>(prob) + 2 * set + 1] = static_cast<double>(cp[pb.n] - cp[0]);
+      }
+    }
+  }
+}
 }  // namespace
 
 namespace nomad {
@@ -500,4 +608,36 @@ cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s) 
   NOMAD_DISPATCH_NV(nv, nomad_dsgd_kernel<float, NV, false><<<grid, wpb * 32, smem, s>>>(a, stratum); return cudaGetLastError());
 }
 
+
+template <typename Store, bool EXACT>
+static cudaError_t batch_epoch_t(const BatchArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = EXACT ? static_cast<size_t>(kBatchThreads / 32) * 128 * sizeof(float) : 0;
+  nomad_batch_kernel<Store, EXACT><<<grid, kBatchThreads, smem, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  batch_advance_kernel<<<1, 1, 0, s>>>(a.epoch, a.next);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_epoch(const BatchArgs& a, int grid, cudaStream_t s) {
+  if (a.bf16) return a.exact ? batch_epoch_t<__nv_bfloat16, true>(a, grid, s) : batch_epoch_t<__nv_bfloat16, false>(a, grid, s);
+  return a.exact ? batch_epoch_t<float, true>(a, grid, s) : batch_epoch_t<float, false>(a, grid, s);
+}
+
+cudaError_t batch_occupancy(int bf16, int exact, int* bps) {
+  const size_t smem = exact ? static_cast<size_t>(kBatchThreads / 32) * 128 * sizeof(float) : 0;
+  if (bf16)
+    return exact ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch_kernel<__nv_bfloat16, true>, kBatchThreads, smem)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch_kernel<__nv_bfloat16, false>, kBatchThreads, smem);
+  return exact ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch_kernel<float, true>, kBatchThreads, smem)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch_kernel<float, false>, kBatchThreads, smem);
+}
+
+cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s) {
+  if (a.bf16)
+    batch_sse_kernel<__nv_bfloat16><<<grid, kBatchThreads, 0, s>>>(a);
+  else
+    batch_sse_kernel<float><<<grid, kBatchThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
 }  // namespace nomad

@@ -77,6 +77,37 @@ struct DsgdArgs {
   int32_t exact = 0;
 };
 
+// Batched problems: one entry per problem of the concatenated storage.
+struct BatchProblem {
+  int64_t w_off, h_off;           // element offsets of the problem's W and H rows
+  int64_t col_off, test_col_off;  // offsets of its n + 1 column pointers (train, test)
+  int32_t m, n, dim, kpad;
+  int32_t nvec, red_width, pad0, pad1;
+};
+static_assert(sizeof(BatchProblem) == 64, "batch problem entry");
+
+struct BatchArgs {
+  void* W = nullptr;  // every problem's rows, concatenated
+  void* H = nullptr;
+  const BatchProblem* problems = nullptr;
+  const int32_t* order = nullptr;  // problems by decreasing rating count (the work queue)
+  int32_t count = 0;
+  const int2* ratings = nullptr;    // train ratings, CSC per problem, concatenated
+  const int64_t* col_ptr = nullptr; // absolute offsets into `ratings`
+  const int2* test = nullptr;
+  const int64_t* test_col_ptr = nullptr;
+  const float* steps = nullptr;     // [n_steps] step size per pass count
+  int32_t n_steps = 0;
+  int32_t* next = nullptr;          // [1] work-queue head
+  int32_t* epoch = nullptr;         // [1] pass count of the next launch
+  float lambda = 0.f;
+  uint32_t seed32 = 0;
+  int32_t bf16 = 0, exact = 0;
+  unsigned long long* stats = nullptr;  // [0] updates
+  double* err_sum = nullptr;            // [1] online squared error
+  double* sse = nullptr;                // [4 * count] train SSE, train count, test SSE, test count
+};
+
 struct SseArgs {
   DevFactors f;
   const int2* ratings = nullptr;
@@ -98,6 +129,12 @@ cudaError_t launch_drain_queues(const AsyncArgs& a, cudaStream_t s);
 cudaError_t launch_build_segx(const int4* segs, const int2* ratings, int64_t nseg, int4* segx, cudaStream_t s);
 cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int cta_heavy, int* blocks_per_sm);
 cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);
+// One epoch of every batched problem (the work-queue kernel, then the pass-count advance);
+// `grid` blocks of kBatchThreads threads.
+constexpr int kBatchThreads = 128;
+cudaError_t launch_batch_epoch(const BatchArgs& a, int grid, cudaStream_t s);
+cudaError_t batch_occupancy(int bf16, int exact, int* blocks_per_sm);
+cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
 cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);
 cudaError_t launch_init_hash(const DevFactors& f, uint64_t seed, cudaStream_t s);

@@ -100,7 +100,8 @@ int ensure_steps(nomad_gpu_batch* b, int32_t needed) {
 int ensure_graph(nomad_gpu_batch* b) {
   if (b->exec) return NOMAD_OK;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  const cudaError_t le = nomad::launch_batch_epoch(b->a, b->grid, b->stream);
+  const cudaError_t le = b->a.exact ? nomad::launch_batch_epoch(b->a, b->grid, b->stream)
+                                    : nomad::launch_batch_epoch2(b->a, b->grid, b->stream);
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
   if (le != cudaSuccess) {
@@ -134,6 +135,8 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   std::vector<nomad::Rating> tr_all, te_all;  // {int32 row, float value}: the device's int2
   std::vector<int64_t> cp_all, tcp_all;
   std::vector<int64_t> nnz(count);
+  std::vector<nomad::Csc> csc_keep;  // large-problem candidates need their CSC below
+  csc_keep.resize(count);
   int64_t w_off = 0, h_off = 0;
   int64_t max_rows = 0;
   for (int32_t i = 0; i < count; ++i) {
@@ -165,11 +168,67 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     tr_all.insert(tr_all.end(), tr.ratings.begin(), tr.ratings.end());
     te_all.insert(te_all.end(), te.ratings.begin(), te.ratings.end());
     nnz[i] = tr.nnz();
+    int32_t act = 0;
+    for (int32_t j = 0; j < q.n; ++j) act += tr.col_ptr[j + 1] > tr.col_ptr[j] ? 1 : 0;
+    pb.n_active = act;
+    csc_keep[i] = std::move(tr);
   }
   // work queue: the largest problems first, so the longest epochs start first
   std::vector<int32_t> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return nnz[x] > nnz[y]; });
+  // FMA form: problems with more than four warps' fair share of the ratings run on a whole
+  // block as NOMAD workers (rows split into kBatchWorkers blocks of equal rating counts)
+  int bps = 0;
+  if (p.exact)
+    CK(nomad::batch_occupancy(bf16, 1, &bps));
+  else
+    CK(nomad::batch2_occupancy(bf16, &bps));
+  if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
+  b->grid = bps * b->num_sms;
+  const int64_t total = std::accumulate(nnz.begin(), nnz.end(), int64_t(0));
+  const int64_t warps = static_cast<int64_t>(b->grid) * (p.exact ? nomad::kBatchThreads / 32 : nomad::kBatchWorkers);
+  const int64_t big_min = std::max<int64_t>(8192, 4 * total / std::max<int64_t>(warps, 1));
+  int32_t n_big = 0;
+  constexpr int R = nomad::kBatchWorkers;
+  std::vector<int32_t> rs_all;
+  std::vector<int64_t> seg_all;
+  if (!p.exact) {
+    while (n_big < count && nnz[order[n_big]] >= big_min && P[order[n_big]].n < nomad::kBatchRing &&
+           P[order[n_big]].n < 65536)
+      ++n_big;
+    for (int32_t t = 0; t < n_big; ++t) {
+      const int32_t i = order[t];
+      const nomad::Csc& c = csc_keep[i];
+      nomad::BatchProblem& pb = b->probs[i];
+      std::vector<int64_t> row_nnz(pb.m, 0);
+      for (const auto& r : c.ratings) ++row_nnz[r.row];
+      pb.rs_off = static_cast<int32_t>(rs_all.size());
+      const int64_t nz = c.nnz();
+      int64_t acc = 0;
+      int32_t r = 1;
+      rs_all.push_back(0);
+      for (int32_t row = 0; row < pb.m && r < R; ++row) {
+        acc += row_nnz[row];
+        while (r < R && acc >= (nz * r + R - 1) / R) {
+          rs_all.push_back(row + 1);
+          ++r;
+        }
+      }
+      for (; r <= R; ++r) rs_all.push_back(pb.m);
+      const int32_t* rs = rs_all.data() + pb.rs_off;
+      pb.seg_off = static_cast<int64_t>(seg_all.size());
+      const int64_t cbase = cp_all[pb.col_off];  // absolute offset of the problem's ratings
+      for (int32_t j = 0; j < pb.n; ++j) {
+        int64_t o = c.col_ptr[j];
+        for (int32_t w = 0; w <= R; ++w) {
+          while (o < c.col_ptr[j + 1] && c.ratings[o].row < rs[w]) ++o;
+          seg_all.push_back(cbase + o);
+        }
+      }
+    }
+  }
+  csc_keep.clear();
 
   nomad::BatchArgs& a = b->a;
   a.count = count;
@@ -204,8 +263,26 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   RC(dalloc(b, &a.stats, 4));
   RC(dalloc(b, &a.err_sum, 1));
   RC(dalloc(b, &a.sse, 4 * static_cast<size_t>(count)));
-  CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), b->stream));
   CK(cudaMemsetAsync(a.epoch, 0, sizeof(int32_t), b->stream));
+  a.n_big = n_big;
+  RC(dalloc(b, &a.next_big, 1));
+  RC(dalloc(b, &a.ctrl, 2));
+  CK(cudaMemsetAsync(a.next_big, 0, sizeof(int32_t), b->stream));
+  CK(cudaMemsetAsync(a.ctrl, 0, 2 * sizeof(int32_t), b->stream));
+  CK(cudaMemcpyAsync(a.next, &a.n_big, sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));  // small ones after
+  a.budget_ns = static_cast<int64_t>(std::max(p.spin_budget_ms, 1)) * 1000000LL;
+  if (n_big > 0) {
+    int32_t* rs = nullptr;
+    int64_t* sg = nullptr;
+    RC(upload(b, &rs, rs_all.data(), rs_all.size()));
+    RC(upload(b, &sg, seg_all.data(), seg_all.size()));
+    a.row_start = rs;
+    a.seg = sg;
+    RC(dalloc(b, &a.rings, static_cast<size_t>(b->grid) * R * nomad::kBatchRing));
+    RC(dalloc(b, &a.ring_ctr, static_cast<size_t>(b->grid) * R));
+    CK(cudaMemsetAsync(a.rings, 0xff, static_cast<size_t>(b->grid) * R * nomad::kBatchRing * 8, b->stream));
+    CK(cudaMemsetAsync(a.ring_ctr, 0, static_cast<size_t>(b->grid) * R * sizeof(unsigned), b->stream));
+  }
 
   // ---- factors: given, or the reference init of each problem, through one staging buffer
   float* stage = nullptr;
@@ -231,10 +308,6 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     }
   }
 
-  int bps = 0;
-  CK(nomad::batch_occupancy(bf16, p.exact, &bps));
-  if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
-  b->grid = bps * b->num_sms;
   b->sse_grid = std::max(1, std::min((count + 3) / 4, 8 * b->num_sms));
   RC(ensure_steps(b, 64));
   CK(cudaStreamSynchronize(b->stream));
@@ -292,6 +365,9 @@ int nomad_gpu_batch_epoch(nomad_gpu_batch* b, int32_t n_epochs, nomad_gpu_epoch_
   CK(cudaStreamSynchronize(b->stream));
   unsigned long long stats[4];
   double esum = 0.0;
+  int32_t ctrl[2] = {0, 0};
+  CK(cudaMemcpy(ctrl, b->a.ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
+  if (ctrl[1] != 0) NOMAD_FAIL(NOMAD_ERR_TIMEOUT, "a large problem's worker waited past the budget");
   CK(cudaMemcpy(stats, b->a.stats, sizeof(stats), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(&esum, b->a.err_sum, sizeof(double), cudaMemcpyDeviceToHost));
   float ms = 0.f;

@@ -552,6 +552,186 @@ __global__ void __launch_bounds__(nomad::kBatchThreads) batch_sse_kernel(nomad::
     }
   }
 }
+
+// ---------------------------------------------------------------------------------
+// FMA form of the batch: a problem with more ratings than a warp's fair share runs on all
+// kBatchWorkers warps of one block as NOMAD workers.  Warp r owns rows
+// [row_start[r], row_start[r+1]); a column token visits the row blocks (j + i) mod R,
+// i = 0..R-1, once per epoch (the reference's routing on one rank, with a rotation in
+// place of the shuffled permutation, nb_main.cpp:551-565).  Tokens move through per-warp
+// rings of sequence-tagged entries in global memory; every producer and consumer is in
+// the block, so block-scope release/acquire orders them and the tail counters are
+// shared-memory atomics.  The ring counters persist across problems and launches, so an
+// old entry never matches.  Other problems run the one-worker schedule on one warp.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ld_acquire_cta_g64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.cta.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta_g64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.cta.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// A large problem's epoch on the block's R warps (all call it; it ends with a barrier).
+template <typename Store>
+__device__ __forceinline__ void batch_large_problem(const nomad::BatchArgs& a, int prob, int ep, float step,
+                                                    double& esum, unsigned long long& n_upd, unsigned* s_tail,
+                                                    int* s_done, int lane, int wib) {
+  constexpr int NV = 1;
+  constexpr int E = Vec<Store>::E;
+  constexpr int R = nomad::kBatchWorkers;
+  constexpr unsigned kMask = nomad::kBatchRing - 1;
+  const nomad::BatchProblem pb = a.problems[prob];
+  const nomad::DevFactors f = batch_factors(a, pb, static_cast<int>(sizeof(Store)));
+  Store* __restrict__ W = static_cast<Store*>(f.W);
+  Store* __restrict__ H = static_cast<Store*>(f.H);
+  const int64_t* seg = a.seg + pb.seg_off;
+  const int64_t* cp = a.col_ptr + pb.col_off;
+  unsigned long long* rings = a.rings + static_cast<int64_t>(blockIdx.x) * R * nomad::kBatchRing;
+  unsigned long long* ring = rings + static_cast<int64_t>(wib) * nomad::kBatchRing;
+  unsigned* ctr = a.ring_ctr + static_cast<int64_t>(blockIdx.x) * R;
+  const uint32_t pkey = nd::hash32(a.seed32 ^ static_cast<uint32_t>(prob) * 0x27D4EB2Fu);
+  // seed this warp's ring: the columns j = wib (mod R) with ratings, in index order
+  const unsigned base = ctr[wib];
+  unsigned k = 0;
+  for (int j0 = wib; j0 < pb.n; j0 += 32 * R) {
+    const int j = j0 + lane * R;
+    const bool has = j < pb.n && cp[j + 1] > cp[j];
+    const unsigned bal = __ballot_sync(kFull, has);
+    if (has) {
+      const unsigned seq = base + k + __popc(bal & ((1u << lane) - 1u));
+      ring[seq & kMask] = (static_cast<unsigned long long>(seq) << 32) | static_cast<unsigned>(j);
+    }
+    k += __popc(bal);
+  }
+  if (lane == 0) s_tail[wib] = base + k;
+  __syncthreads();  // every ring seeded; s_done was cleared before the caller's barrier
+  unsigned head = base, backoff = 32;
+  uint64_t idle_since = 0;
+  while (true) {
+    unsigned long long e = 0;
+    if (lane == 0) e = ld_acquire_cta_g64(ring + (head & kMask));
+    const unsigned hi = __shfl_sync(kFull, static_cast<unsigned>(e >> 32), 0);
+    const unsigned lo = __shfl_sync(kFull, static_cast<unsigned>(e), 0);
+    if (hi == head && !(lo & 0x80000000u)) {
+      __syncwarp();
+      ++head;
+      const int j = static_cast<int>(lo & 0xffffu), pos = static_cast<int>(lo >> 16);
+      const int64_t b = seg[static_cast<int64_t>(j) * (R + 1) + wib];
+      const int64_t en = seg[static_cast<int64_t>(j) * (R + 1) + wib + 1];
+      if (en > b) {
+        const uint32_t colkey = nd::hash32(pkey ^ static_cast<uint32_t>(j) * 0x85EBCA77u ^
+                                           static_cast<uint32_t>(ep) * 0xC2B2AE3Du);
+        float h[NV][E];
+        const Store* hrow = H + static_cast<int64_t>(j) * f.kpad;  // last written by a warp of this block
+        if (lane < f.nvec) nd::load_vec<Store>(hrow, lane, h[0]);
+        else
+#pragma unroll
+          for (int i = 0; i < E; ++i) h[0][i] = 0.f;
+        esum += visit_segment<Store, NV, false, 2>(W, f, h, a.ratings, b, static_cast<int>(en - b), step, a.lambda,
+                                                   colkey, lane, nullptr);
+        store_col<Store, NV>(H, j, f, lane, h, nd::hash32(colkey));
+        n_upd += static_cast<unsigned long long>(en - b);
+      }
+      __syncwarp();  // the column's stores precede lane 0's release
+      if (lane == 0) {
+        if (pos + 1 < R) {
+          const int nr = (j + pos + 1) % R;
+          const unsigned seq = atomicAdd(&s_tail[nr], 1u);
+          st_release_cta_g64(rings + static_cast<int64_t>(nr) * nomad::kBatchRing + (seq & kMask),
+                             (static_cast<unsigned long long>(seq) << 32) |
+                                 static_cast<unsigned>(j | ((pos + 1) << 16)));
+        } else {
+          atomicAdd(s_done, 1);
+        }
+      }
+      backoff = 32;
+      idle_since = 0;
+    } else {
+      int fin = 0;
+      if (lane == 0) {
+        fin = *reinterpret_cast<volatile int*>(s_done) >= pb.n_active;
+        const uint64_t now = nd::globaltimer();
+        if (!fin) {
+          if (idle_since == 0) {
+            idle_since = now;
+          } else if (static_cast<int64_t>(now - idle_since) > a.budget_ns) {
+            atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
+            fin = 1;
+          }
+        }
+      }
+      if (__shfl_sync(kFull, fin, 0)) break;
+      __nanosleep(backoff);
+      backoff = min(backoff * 2, 256u);
+    }
+  }
+  if (lane == 0) ctr[wib] = head;
+  __syncthreads();
+}
+
+template <typename Store>
+__global__ void __launch_bounds__(nomad::kBatchWorkers * 32, 1) nomad_batch2_kernel(nomad::BatchArgs a) {
+  constexpr int NV = 1;
+  constexpr int E = Vec<Store>::E;
+  __shared__ unsigned s_tail[nomad::kBatchWorkers];
+  __shared__ int s_done, s_big;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int ep = *a.epoch;
+  const float step = a.steps[min(ep, a.n_steps - 1)];
+  double esum = 0.0;
+  unsigned long long n_upd = 0;
+  // large problems, a block each
+  while (true) {
+    if (threadIdx.x == 0) {  // one thread decides for the block, so every thread leaves together
+      s_big = nd::ld_acquire(&a.ctrl[1]) != 0 ? a.n_big : atomicAdd(a.next_big, 1);
+      s_done = 0;
+    }
+    __syncthreads();
+    const int q = s_big;
+    if (q >= a.n_big) break;
+    batch_large_problem<Store>(a, a.order[q], ep, step, esum, n_upd, s_tail, &s_done, lane, wib);
+  }
+  // the rest, a warp each: the one-worker schedule in FMA arithmetic
+  while (true) {
+    int p = 0;
+    if (lane == 0) p = atomicAdd(a.next, 1);
+    p = __shfl_sync(kFull, p, 0);
+    if (p >= a.count) break;
+    const int prob = a.order[p];
+    const nomad::BatchProblem pb = a.problems[prob];
+    const nomad::DevFactors f = batch_factors(a, pb, static_cast<int>(sizeof(Store)));
+    Store* __restrict__ W = static_cast<Store*>(f.W);
+    Store* __restrict__ H = static_cast<Store*>(f.H);
+    const int64_t* cp = a.col_ptr + pb.col_off;
+    const uint32_t pkey = nd::hash32(a.seed32 ^ static_cast<uint32_t>(prob) * 0x27D4EB2Fu);
+    for (int j = 0; j < pb.n; ++j) {
+      const int64_t b = cp[j], e = cp[j + 1];
+      if (b == e) continue;
+      const uint32_t colkey = nd::hash32(pkey ^ static_cast<uint32_t>(j) * 0x85EBCA77u ^
+                                         static_cast<uint32_t>(ep) * 0xC2B2AE3Du);
+      float h[NV][E];
+      load_col<Store, NV>(H, j, f, lane, h);
+      esum += visit_segment<Store, NV, false, 2>(W, f, h, a.ratings, b, static_cast<int>(e - b), step, a.lambda,
+                                                 colkey, lane, nullptr);
+      store_col<Store, NV>(H, j, f, lane, h, nd::hash32(colkey));
+      n_upd += static_cast<unsigned long long>(e - b);
+      __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    atomicAdd(&a.stats[0], n_upd);
+    atomicAdd(a.err_sum, esum);
+  }
+}
+
+__global__ void batch2_advance_kernel(int32_t* epoch, int32_t* next, int32_t* next_big, int32_t n_big) {
+  *epoch += 1;
+  *next = n_big;
+  *next_big = 0;
+}
 }  // namespace
 
 namespace nomad {
@@ -639,5 +819,24 @@ cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s) {
   else
     batch_sse_kernel<float><<<grid, kBatchThreads, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+template <typename Store>
+static cudaError_t batch_epoch2_t(const BatchArgs& a, int grid, cudaStream_t s) {
+  nomad_batch2_kernel<Store><<<grid, kBatchWorkers * 32, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  batch2_advance_kernel<<<1, 1, 0, s>>>(a.epoch, a.next, a.next_big, a.n_big);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_epoch2(const BatchArgs& a, int grid, cudaStream_t s) {
+  return a.bf16 ? batch_epoch2_t<__nv_bfloat16>(a, grid, s) : batch_epoch2_t<float>(a, grid, s);
+}
+
+cudaError_t batch2_occupancy(int bf16, int* bps) {
+  return bf16 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<__nv_bfloat16>,
+                                                              kBatchWorkers * 32, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<float>, kBatchWorkers * 32, 0);
 }
 }  // namespace nomad

@@ -82,9 +82,18 @@ struct BatchProblem {
   int64_t w_off, h_off;           // element offsets of the problem's W and H rows
   int64_t col_off, test_col_off;  // offsets of its n + 1 column pointers (train, test)
   int32_t m, n, dim, kpad;
-  int32_t nvec, red_width, pad0, pad1;
+  int32_t nvec, red_width;
+  int32_t rs_off;                 // large problems: offset of the warps' row-block bounds
+  int32_t n_active;               // columns with training ratings
+  int64_t seg_off;                // large problems: offset of the n x (R + 1) visit bounds
+  int64_t pad;
 };
-static_assert(sizeof(BatchProblem) == 64, "batch problem entry");
+static_assert(sizeof(BatchProblem) == 80, "batch problem entry");
+
+// Large batched problems run on every warp of a block as NOMAD workers; the row blocks
+// and the column visit bounds are laid out for this many warps.
+constexpr int kBatchWorkers = 16;
+constexpr int kBatchRing = 8192;  // ring capacity: a large problem has at most 5,000 + columns
 
 struct BatchArgs {
   void* W = nullptr;  // every problem's rows, concatenated
@@ -106,6 +115,15 @@ struct BatchArgs {
   unsigned long long* stats = nullptr;  // [0] updates
   double* err_sum = nullptr;            // [1] online squared error
   double* sse = nullptr;                // [4 * count] train SSE, train count, test SSE, test count
+  // large problems: the first n_big entries of `order`, taken a block at a time
+  int32_t n_big = 0;
+  int32_t* next_big = nullptr;          // [1] large-problem queue head
+  const int32_t* row_start = nullptr;   // per large problem: kBatchWorkers + 1 row bounds
+  const int64_t* seg = nullptr;         // per large problem: n x (kBatchWorkers + 1) rating offsets
+  unsigned long long* rings = nullptr;  // [grid x kBatchWorkers x kBatchRing] token rings
+  unsigned* ring_ctr = nullptr;         // [grid x kBatchWorkers] ring counters (persist)
+  int32_t* ctrl = nullptr;              // [2]: [1] device status (a large problem's wait ran out)
+  int64_t budget_ns = 0;                // bound of a worker's idle wait inside a large problem
 };
 
 struct SseArgs {
@@ -134,6 +152,10 @@ cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);
 constexpr int kBatchThreads = 128;
 cudaError_t launch_batch_epoch(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t batch_occupancy(int bf16, int exact, int* blocks_per_sm);
+// FMA form: blocks of kBatchWorkers warps; large problems first (a block each), then the
+// rest a warp each.
+cudaError_t launch_batch_epoch2(const BatchArgs& a, int grid, cudaStream_t s);
+cudaError_t batch2_occupancy(int bf16, int* blocks_per_sm);
 cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
 cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);

@@ -297,7 +297,8 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       pri_min = std::max<int64_t>(1, c->max_column * permille / 1000);
     }
     nomad::AsyncLayout L;
-    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, cta_heavy ? c->wpb : 1, L, threads));
+    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, p.exact ? 1 : c->wpb, !p.exact, L,
+                                 threads));
     c->cta_heavy = cta_heavy && pri_min > 0;
     c->n_active = L.n_active;
     c->n_priority = L.n_priority;

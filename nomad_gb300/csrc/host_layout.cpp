@@ -149,7 +149,8 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
 }
 
 int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
-                       int64_t priority_min, int32_t group, AsyncLayout& L, int threads) {
+                       int64_t priority_min, int32_t group, bool group_routes, AsyncLayout& L,
+                       int threads) {
   const int32_t m = csc.m, n = csc.n;
   const int64_t nnz = csc.nnz();
   if (P <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker count must be positive");
@@ -233,6 +234,21 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
       // a random permutation of the workers; empty visits are skipped here)
       SplitMix64 rng(stream_key(seed, 137, static_cast<uint64_t>(j)));
       for (int64_t i = k - 1; i > 0; --i) std::swap(s[i], s[rng.below(i + 1)]);
+      if (group_routes && !pri && group > 1 && k > 1) {
+        // hierarchical route: the visits to one group's workers (a thread block) stay
+        // consecutive, like the reference's token that makes its round of one machine's
+        // threads before it leaves for another machine (nb_main.cpp:551-565); groups and
+        // workers in a group in seeded random order
+        const uint64_t kb = stream_key(seed, 149, static_cast<uint64_t>(j));
+        const uint64_t kw = stream_key(seed, 151, static_cast<uint64_t>(j));
+        std::sort(s, s + k, [&](const Segment& x, const Segment& y) {
+          const uint64_t bx = SplitMix64::mix(kb ^ static_cast<uint64_t>(x.worker / group));
+          const uint64_t by = SplitMix64::mix(kb ^ static_cast<uint64_t>(y.worker / group));
+          if (bx != by) return bx < by;
+          return SplitMix64::mix(kw ^ static_cast<uint64_t>(x.worker)) <
+                 SplitMix64::mix(kw ^ static_cast<uint64_t>(y.worker));
+        });
+      }
     }
   });
   L.max_segment = *std::max_element(maxseg.begin(), maxseg.end());

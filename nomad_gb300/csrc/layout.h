@@ -68,9 +68,11 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
 // priority_min: columns with at least this many ratings use the priority queues
 // (<= 0: none).  group: a priority column visits groups of `group` consecutive workers
 // (the warps of one thread block, which process the visit together); its segments name
-// the group, and its queue is P + group index.
+// the group, and its queue is P + group index.  group_routes: the other columns' routes
+// keep the visits to one group's workers consecutive.
 int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
-                       int64_t priority_min, int32_t group, AsyncLayout& out, int threads);
+                       int64_t priority_min, int32_t group, bool group_routes, AsyncLayout& out,
+                       int threads);
 
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
                       DsgdLayout& out);

@@ -134,16 +134,26 @@ __device__ __forceinline__ uint4 zero_raw<uint4>() { return make_uint4(0u, 0u, 0
 template <>
 __device__ __forceinline__ uint2 zero_raw<uint2>() { return make_uint2(0u, 0u); }
 
+// Stochastic-rounding key of a factor row written during one visit: distinct rows and
+// visits give distinct keys; the hash of key + vector index supplies the random bits.
+__device__ __forceinline__ uint32_t row_key(int row, uint32_t colkey) {
+  return static_cast<uint32_t>(row) * 0x9E3779B1u ^ colkey;
+}
+
 // fp32 values to the stored form; bf16 uses stochastic rounding keyed by `key`
-// (the caller makes keys distinct per row, update and vector).
+// (the caller makes keys distinct per row, update and vector).  One hash per vector: its
+// two halves round the first two values, and the high halves of its products with two
+// odd constants (bijections of the hash, so again uniform) round the other two.  The
+// bits of one vector are correlated, which leaves each value's rounding unbiased.
 __device__ __forceinline__ uint4 pack_raw(const float (&x)[4], uint32_t, uint4*) {
   return make_uint4(__float_as_uint(x[0]), __float_as_uint(x[1]), __float_as_uint(x[2]),
                     __float_as_uint(x[3]));
 }
 __device__ __forceinline__ uint2 pack_raw(const float (&x)[4], uint32_t key, uint2*) {
-  const uint32_t r0 = hash32(key), r1 = hash32(key + 1u);
+  const uint32_t r0 = hash32(key);
+  const uint32_t r1 = r0 * 0x9E3779B1u, r2 = r0 * 0x85EBCA77u;
   const uint32_t a = f32_to_bf16_sr_bits(x[0], r0) & 0xffffu, b = f32_to_bf16_sr_bits(x[1], r0 >> 16);
-  const uint32_t c = f32_to_bf16_sr_bits(x[2], r1) & 0xffffu, d = f32_to_bf16_sr_bits(x[3], r1 >> 16);
+  const uint32_t c = f32_to_bf16_sr_bits(x[2], r1 >> 16) & 0xffffu, d = f32_to_bf16_sr_bits(x[3], r2 >> 16);
   return make_uint2(a | (b << 16), c | (d << 16));
 }
 

@@ -201,7 +201,7 @@ __device__ __forceinline__ float visit_short(const SlotHdr* hd, int len, float (
             w[q][e] = fmaf(-step, fmaf(err, ho, lambda * wo), wo);
             h[q][e] = fmaf(-step, fmaf(err, wo, lambda * ho), ho);
           }
-        store_row<Store, NV>(W, rt.x, s, lane, w, nd::hash32(static_cast<uint32_t>(rt.x) * 0x9E3779B1u ^ colkey));
+        store_row<Store, NV>(W, rt.x, s, lane, w, nd::row_key(rt.x, colkey));
         const int tn = t + kPF;
         if (tn < len) load_row_regs<Store, NV>(W, hd->rv[tn].x, s, lane, wb[i]);
       }
@@ -407,7 +407,7 @@ __device__ __forceinline__ float visit_long(const SlotHdr* hd, int64_t start, in
             h[q][e] = fmaf(ne, wo[e], c * h[q][e]);
           }
         }
-        store_row<Store, NV>(W, rr[t], s, lane, wn, nd::hash32(static_cast<uint32_t>(rr[t]) * 0x9E3779B1u ^ colkey));
+        store_row<Store, NV>(W, rr[t], s, lane, wn, nd::row_key(rr[t], colkey));
       }
     }
     if ((b & 3) == 3) {  // after the fourth block of a chunk: the next rating chunk
@@ -703,7 +703,7 @@ __device__ __forceinline__ void cta_rows(const char* X, int sw, const int2* rvb,
       }
     }
     const int r = rvb[t].x;
-    store_row<Store, NV>(W, r, s, lane, wn, nd::hash32(static_cast<uint32_t>(r) * 0x9E3779B1u ^ colkey));
+    store_row<Store, NV>(W, r, s, lane, wn, nd::row_key(r, colkey));
   }
   if (last) {
 #pragma unroll

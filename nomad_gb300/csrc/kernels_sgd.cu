@@ -143,7 +143,7 @@ __device__ __forceinline__ float visit_segment(Store* __restrict__ W, const noma
           seg_err += err * err;
           apply_update<Store, NV, EXACT>(h, w, err, step, lambda);
           store_row<Store, NV>(W, r, f.kpad, f.nvec, lane, w,
-                               nd::hash32(static_cast<uint32_t>(r) * 0x9E3779B1u ^ colkey));
+                               nd::row_key(r, colkey));
           const int tn = t + PF;
           const int rn = __shfl_sync(kFull, rv.x, tn & 31);
           if (tn < cnt) load_row_raw<Store, NV>(W, rn, f.kpad, f.nvec, lane, wbuf[i]);

@@ -18,6 +18,11 @@
  *   nomad_gpu_get_factors  the --output dump of rows and columns
  *                          (nb_main.cpp:349-366, 683-705)
  *   nomad_gpu_destroy      teardown (nb_main.cpp:368-408)
+ *   nomad_gpu_save_checkpoint / nomad_gpu_load_checkpoint
+ *                          a checkpoint taken at an epoch boundary
+ *                          (NomadBody::archive_local, nb_checkpoint.cpp:47-59) and
+ *                          the --recover path (NomadBody::restore,
+ *                          nb_checkpoint.cpp:135-143; nb_main.cpp:446-449)
  */
 #ifndef NOMAD_GPU_H_
 #define NOMAD_GPU_H_
@@ -171,6 +176,23 @@ int nomad_gpu_get_factors(nomad_gpu_ctx* ctx, float* W, float* H);
 
 /* Overwrite the factors from host float arrays (either may be NULL). */
 int nomad_gpu_set_factors(nomad_gpu_ctx* ctx, const float* W, const float* H);
+
+/* Set the cumulative pass count, the quantity the step size of the next epoch is
+ * computed from (nb_main.cpp:514-515): the next nomad_gpu_epoch runs pass
+ * epochs_done + 1.  Used when training resumes from saved factors. */
+int nomad_gpu_set_epochs_done(nomad_gpu_ctx* ctx, int32_t epochs_done);
+
+/* Write the context's factors and pass count to a checkpoint file (the format of
+ * nomad_io_write_checkpoint).  Between nomad_gpu_epoch calls every column token has
+ * finished its pass, so this is the whole training state.  BF16 factors are widened
+ * to fp32 exactly. */
+int nomad_gpu_save_checkpoint(nomad_gpu_ctx* ctx, const char* path);
+
+/* Restore factors and pass count from a checkpoint file written for a problem of the
+ * same m, n and dim (NOMAD_ERR_INVALID_ARG otherwise).  A REPLAY or DSGD context
+ * restored from the checkpoint of epoch k and run for e epochs ends with the same
+ * factors, bit for bit, as one that ran k + e epochs without stopping. */
+int nomad_gpu_load_checkpoint(nomad_gpu_ctx* ctx, const char* path);
 
 /* Describe the context (sizes, workers, segments, memory). */
 int nomad_gpu_get_info(nomad_gpu_ctx* ctx, nomad_gpu_info* info);

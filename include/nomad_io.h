@@ -15,6 +15,10 @@
  *                          nb_main.cpp:70-92 (values only)
  *   nomad_synth_generate   Code/nomad/synthgen.cpp:180-327 (planted-factor ratings
  *                          from degree laws); a new generator, not a port
+ *   nomad_io_write_checkpoint / nomad_io_read_checkpoint(_header)
+ *                          NomadBody::archive_local / restore_local
+ *                          (nb_checkpoint.cpp:47-59, 114-120), one file per
+ *                          checkpoint instead of one per worker thread
  */
 #ifndef NOMAD_IO_H_
 #define NOMAD_IO_H_
@@ -63,6 +67,31 @@ void nomad_io_free(nomad_io_matrix* mat);
  * (6 significant digits), as the reference's --output writes them. */
 int nomad_io_write_factors(const char* path, int32_t m, int32_t n, int32_t dim,
                            const float* W, const float* H);
+
+/* Checkpoint file: the whole training state at an epoch boundary, where every column
+ * token has finished its pass, so no token is in flight and the factors plus the pass
+ * count are all there is to keep (the reference also archives the column messages
+ * queued at the cut, nb_checkpoint.cpp:61-102; at an epoch boundary there are none).
+ * Layout, little-endian:
+ *   char     magic[8] = "NOMADCP1"
+ *   int32    m, n, dim, epochs_done
+ *   uint64   FNV-1a 64 hash of the W and H bytes that follow
+ *   float32  W[m * dim], H[n * dim]   (row-major)
+ * The file is written under path + ".tmp" and renamed over path, so a crash while
+ * writing leaves an existing checkpoint at path intact. */
+int nomad_io_write_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim,
+                              int32_t epochs_done, const float* W, const float* H);
+
+/* Sizes and pass count of a checkpoint file (any output may be NULL).
+ * NOMAD_ERR_FORMAT when the magic or the sizes are wrong. */
+int nomad_io_read_checkpoint_header(const char* path, int32_t* m, int32_t* n, int32_t* dim,
+                                    int32_t* epochs_done);
+
+/* Read a checkpoint whose sizes must equal m, n, dim (else NOMAD_ERR_INVALID_ARG).
+ * NOMAD_ERR_FORMAT when the file is short, longer than its sizes say, or its hash
+ * does not match.  W or H may be NULL to skip it (the hash is still checked). */
+int nomad_io_read_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim,
+                             float* W, float* H, int32_t* epochs_done);
 
 /* The reference's initial factors, single rank: rows in init_parts blocks of
  * ceil(m/init_parts), block t drawn from mt19937_64(seed + t + 1); columns from

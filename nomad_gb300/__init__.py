@@ -152,6 +152,28 @@ def write_factors(path, W, H):
                                        _ptr(W), _ptr(H)), "nomad_io_write_factors")
 
 
+def write_checkpoint(path, W, H, epochs_done):
+    """Checkpoint file of factors W[m,dim], H[n,dim] after `epochs_done` passes."""
+    W = np.ascontiguousarray(W, np.float32)
+    H = np.ascontiguousarray(H, np.float32)
+    check(lib().nomad_io_write_checkpoint(os.fsencode(path), W.shape[0], H.shape[0], W.shape[1],
+                                          epochs_done, _ptr(W), _ptr(H)),
+          "nomad_io_write_checkpoint")
+
+
+def read_checkpoint(path):
+    """(W, H, epochs_done) from a checkpoint file."""
+    m, n, dim, ep = (ctypes.c_int32() for _ in range(4))
+    check(lib().nomad_io_read_checkpoint_header(os.fsencode(path), ctypes.byref(m), ctypes.byref(n),
+                                                ctypes.byref(dim), ctypes.byref(ep)),
+          "nomad_io_read_checkpoint_header")
+    W = np.empty((m.value, dim.value), np.float32)
+    H = np.empty((n.value, dim.value), np.float32)
+    check(lib().nomad_io_read_checkpoint(os.fsencode(path), m.value, n.value, dim.value, _ptr(W),
+                                         _ptr(H), ctypes.byref(ep)), "nomad_io_read_checkpoint")
+    return W, H, ep.value
+
+
 def default_params(**overrides):
     p = _abi.Params()
     check(lib().nomad_gpu_params_default(ctypes.byref(p)), "nomad_gpu_params_default")
@@ -217,6 +239,17 @@ class Nomad:
         W = None if W is None else np.ascontiguousarray(W, np.float32)
         H = None if H is None else np.ascontiguousarray(H, np.float32)
         check(lib().nomad_gpu_set_factors(self._ctx, _ptr(W), _ptr(H)), "nomad_gpu_set_factors")
+
+    def set_epochs_done(self, epochs_done):
+        check(lib().nomad_gpu_set_epochs_done(self._ctx, epochs_done), "nomad_gpu_set_epochs_done")
+
+    def save_checkpoint(self, path):
+        check(lib().nomad_gpu_save_checkpoint(self._ctx, os.fsencode(path)),
+              "nomad_gpu_save_checkpoint")
+
+    def load_checkpoint(self, path):
+        check(lib().nomad_gpu_load_checkpoint(self._ctx, os.fsencode(path)),
+              "nomad_gpu_load_checkpoint")
 
     def token_finish_times(self):
         """Seconds from the last ASYNC epoch launch's start to each token's last pass."""

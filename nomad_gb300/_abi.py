@@ -105,6 +105,9 @@ SIGNATURES = {
     "nomad_gpu_get_factors": (ctypes.c_int, [c_vp, c_vp, c_vp]),
     "nomad_gpu_set_factors": (ctypes.c_int, [c_vp, c_vp, c_vp]),
     "nomad_gpu_get_info": (ctypes.c_int, [c_vp, ctypes.POINTER(Info)]),
+    "nomad_gpu_set_epochs_done": (ctypes.c_int, [c_vp, c_i32]),
+    "nomad_gpu_save_checkpoint": (ctypes.c_int, [c_vp, ctypes.c_char_p]),
+    "nomad_gpu_load_checkpoint": (ctypes.c_int, [c_vp, ctypes.c_char_p]),
     "nomad_gpu_destroy": (None, [c_vp]),
     "nomad_gpu_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "nomad_gpu_last_error": (ctypes.c_char_p, []),
@@ -129,6 +132,13 @@ SIGNATURES = {
     "nomad_io_free": (None, [ctypes.POINTER(IoMatrix)]),
     "nomad_io_write_factors": (ctypes.c_int, [ctypes.c_char_p, c_i32, c_i32, c_i32, c_vp,
                                               c_vp]),
+    "nomad_io_write_checkpoint": (ctypes.c_int, [ctypes.c_char_p, c_i32, c_i32, c_i32, c_i32,
+                                                 c_vp, c_vp]),
+    "nomad_io_read_checkpoint_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_i32),
+                                                       ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
+                                                       ctypes.POINTER(c_i32)]),
+    "nomad_io_read_checkpoint": (ctypes.c_int, [ctypes.c_char_p, c_i32, c_i32, c_i32, c_vp, c_vp,
+                                                ctypes.POINTER(c_i32)]),
     "nomad_reference_init": (ctypes.c_int, [c_i32, c_i32, c_i32, c_u64, c_i32, c_vp, c_vp]),
     "nomad_synth_preset": (ctypes.c_int, [c_i32, ctypes.POINTER(SynthSpec)]),
     "nomad_synth_generate": (ctypes.c_int, [ctypes.POINTER(SynthSpec),

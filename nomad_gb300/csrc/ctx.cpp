@@ -659,6 +659,34 @@ int nomad_gpu_set_factors(nomad_gpu_ctx* c, const float* W, const float* H) {
   return NOMAD_OK;
 }
 
+int nomad_gpu_set_epochs_done(nomad_gpu_ctx* c, int32_t epochs_done) {
+  nomad::clear_last_error();
+  if (!c || epochs_done < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
+  CK(cudaSetDevice(c->device));
+  c->epochs_done = epochs_done;
+  // the exact kernel keeps each token's pass count on the device between calls
+  if (c->tok_epoch) RC(reset_tokens(c));
+  return NOMAD_OK;
+}
+
+int nomad_gpu_save_checkpoint(nomad_gpu_ctx* c, const char* path) {
+  nomad::clear_last_error();
+  if (!c || !path) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
+  std::vector<float> W(static_cast<size_t>(c->f.m) * c->f.dim), H(static_cast<size_t>(c->f.n) * c->f.dim);
+  RC(nomad_gpu_get_factors(c, W.data(), H.data()));
+  return nomad_io_write_checkpoint(path, c->f.m, c->f.n, c->f.dim, c->epochs_done, W.data(), H.data());
+}
+
+int nomad_gpu_load_checkpoint(nomad_gpu_ctx* c, const char* path) {
+  nomad::clear_last_error();
+  if (!c || !path) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
+  std::vector<float> W(static_cast<size_t>(c->f.m) * c->f.dim), H(static_cast<size_t>(c->f.n) * c->f.dim);
+  int32_t ep = 0;
+  RC(nomad_io_read_checkpoint(path, c->f.m, c->f.n, c->f.dim, W.data(), H.data(), &ep));
+  RC(nomad_gpu_set_factors(c, W.data(), H.data()));
+  return nomad_gpu_set_epochs_done(c, ep);
+}
+
 int nomad_gpu_get_info(nomad_gpu_ctx* c, nomad_gpu_info* info) {
   if (!c || !info) return NOMAD_ERR_INVALID_ARG;
   std::memset(info, 0, sizeof(*info));

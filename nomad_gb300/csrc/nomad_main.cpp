@@ -7,6 +7,20 @@
 // The timeout list is cumulative wall-clock seconds of training, as in the reference
 // (nb_main.cpp:109-113); training advances in whole epochs and the budget is checked
 // between epochs.  --epochs N trains exactly N epochs per timeout point instead.
+//
+// Online termination follows NomadBody::master_termcheck (nb_master.cpp:16-46): every
+// --tm_interval seconds of training the online RMSE, sqrt(sum of the squared errors the
+// column tokens saw on their latest pass / training nnz), is compared with the previous
+// check; training stops for good once it changed by at most --tm_error, or once it is
+// at most --tm_value after 8 passes of every column (the reference's 8 * machines *
+// columns column sends: one send per machine per pass).
+//
+// Checkpoints (--cptype, --cpinterval, --cppath) are taken between epochs, every
+// --cpinterval seconds of training, as <cppath>/cp-t<jobid>-e<k>.ckpt; --recover k
+// resumes from one (nb_master.cpp:69-104, nb_checkpoint.cpp:37-42, nb_main.cpp:446-449).
+// Between epochs no column token is in flight, so the reference's sync, async and vs
+// protocols, which differ in how they capture messages in flight, all save the same
+// state here: the factors and the pass count.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -14,6 +28,7 @@
 #include <cstring>
 #include <iomanip>
 #include <iostream>
+#include <limits>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -60,10 +75,12 @@ const char* kUsage =
     "  --cpm arg (=100)             accepted for compatibility (single GPU: no messages)\n"
     "  --tpm arg (=0.5)             accepted for compatibility\n"
     "  -t [ --timeout ] arg (=10.0) timeout seconds until completion (cumulative list)\n"
-    "  -u [ --tm_value ] arg (=1)   accepted for compatibility\n"
-    "  -e [ --tm_error ] arg (=1e-6) accepted for compatibility\n"
-    "  --tm_interval arg (=1)       accepted for compatibility\n"
-    "  --tm_portion arg (=0.01)     accepted for compatibility\n"
+    "  -u [ --tm_value ] arg (=1)   stop when the online RMSE is at most this (after 8\n"
+    "                               passes of every column)\n"
+    "  -e [ --tm_error ] arg (=1e-6) stop when the online RMSE changes by at most this\n"
+    "                               between two checks\n"
+    "  --tm_interval arg (=1)       seconds of training between termination checks\n"
+    "  --tm_portion arg (=0.01)     accepted for compatibility (checks see whole passes)\n"
     "  --dim arg (=100)             dimension of latent space\n"
     "  --reuse arg (=1)             number of column reuse (only 1 is supported)\n"
     "  --pause arg (=1)             pause 3 s after each timeout point\n"
@@ -72,11 +89,12 @@ const char* kUsage =
     "  -i [ --input ] arg           path of data (train.dat, test.dat)\n"
     "  --path arg                   path of data (legacy name of --input)\n"
     "  -o [ --output ] arg          prefix of the factor dump (<output>0)\n"
-    "  --recover arg (=-1)          accepted for compatibility (no checkpoints)\n"
-    "  -j [ --jobid ] arg (=1)      accepted for compatibility\n"
-    "  -c [ --cptype ] arg (=none)  checkpoint type: only none is supported\n"
-    "  -k [ --cpinterval ] arg (=0) accepted for compatibility\n"
-    "  -p [ --cppath ] arg          accepted for compatibility\n"
+    "  --recover arg (=-1)          resume from checkpoint arg (-1 means do not recover)\n"
+    "  -j [ --jobid ] arg (=1)      job id in checkpoint file names\n"
+    "  -c [ --cptype ] arg (=none)  type of checkpoint (none, sync, async, vs); all are\n"
+    "                               taken between epochs\n"
+    "  -k [ --cpinterval ] arg (=0) seconds of training between checkpoints\n"
+    "  -p [ --cppath ] arg          directory of checkpoint files\n"
     "  --net_delay arg (=0)         accepted for compatibility\n"
     "  --net_ratio arg (=inf)       accepted for compatibility\n"
     "  -v [ --verbose ] arg (=0)    verbose level\n"
@@ -212,7 +230,8 @@ bool parse(int argc, char** argv, Options& o, bool& help) {
   if (o.cptype != "none" && o.cptype != "sync" && o.cptype != "async" && o.cptype != "vs") {
     std::cerr << "checkpoint type is inalid.\n"; ok = false;
   }
-  if (o.cptype != "none") { std::cerr << "checkpointing is not supported by this build.\n"; ok = false; }
+  if (o.cptype != "none" && o.cpinterval <= 0) { std::cerr << "checkpoint interval is invalid.\n"; ok = false; }
+  if (o.cptype != "none" && o.cppath.empty()) { std::cerr << "checkpoint path is not given.\n"; ok = false; }
   if (o.reuse != 1) { std::cerr << "only --reuse 1 is supported.\n"; ok = false; }
   if (o.mode != "async" && o.mode != "dsgd" && o.mode != "replay") { std::cerr << "unknown --mode.\n"; ok = false; }
   if (o.precision != "fp32" && o.precision != "bf16") { std::cerr << "unknown --precision.\n"; ok = false; }
@@ -269,22 +288,77 @@ int main(int argc, char** argv) {
     nomad_io_free(&test);
     return 1;
   }
+  std::string cp_dir = o.cppath.empty() ? "" : o.cppath + "/";
+  auto cp_file = [&](int k) { return cp_dir + "cp-t" + std::to_string(o.jobid) + "-e" + std::to_string(k) + ".ckpt"; };
+  int cp_epoch = 0;  // number of the next checkpoint
+  if (o.recover >= 0) {
+    const std::string f = cp_file(o.recover);
+    rc = nomad_gpu_load_checkpoint(ctx, f.c_str());
+    if (rc) {
+      std::cerr << "error in restoring checkpoint " << f << ": " << nomad_gpu_last_error() << "\n";
+      nomad_gpu_destroy(ctx);
+      nomad_io_free(&train);
+      nomad_io_free(&test);
+      return 1;
+    }
+    cp_epoch = o.recover + 1;
+  }
   for (double t : o.timeouts) std::cerr << "timeout: " << t << "\n";
   double train_time = 0, test_time = 0;
   long long updates = 0, failures = 0, sends = 0;
-  for (size_t it = 0; it < o.timeouts.size() && rc == NOMAD_OK; ++it) {
+  // online termination state (nb_master.cpp:18-20)
+  const long long mini_stop_passes = 8LL * train.n;
+  long long passes = 0;
+  double global_error = std::numeric_limits<double>::infinity(), last_check = 0;
+  bool finished = false;
+  // checkpoint state
+  const bool checkpointing = o.cptype != "none";
+  double last_cp = 0, cp_time = 0;
+  int cp_count = 0;
+  for (size_t it = 0; it < o.timeouts.size() && rc == NOMAD_OK && !finished; ++it) {
     // train until the cumulative training time reaches this timeout point
     const auto t0 = std::chrono::steady_clock::now();
+    auto elapsed = [&] { return train_time + std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
     int done_here = 0;
     while (rc == NOMAD_OK) {
-      const double elapsed = train_time + std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-      if (o.epochs > 0 ? done_here >= o.epochs : elapsed >= o.timeouts[it]) break;
+      if (o.epochs > 0 ? done_here >= o.epochs : elapsed() >= o.timeouts[it]) break;
       nomad_gpu_epoch_stats st;
       rc = nomad_gpu_epoch(ctx, 1, &st);
+      if (rc) break;
       updates += st.updates;
       failures += st.failures;
       sends += st.hops;
+      passes += train.n;  // one pass of every column token
       ++done_here;
+      const double now = elapsed();
+      if (now - last_check >= o.tm_interval) {
+        // NomadBody::master_termcheck: one check (nb_master.cpp:35-44)
+        last_check = now;
+        const double rmse = std::sqrt(st.online_sse / static_cast<double>(std::max<int64_t>(train.nnz, 1)));
+        const double diff = std::fabs(rmse - global_error);
+        std::cerr << "M: termination check at " << std::fixed << std::setprecision(2) << now
+                  << ": RMSE: " << std::setprecision(12) << rmse << ", difference: " << std::defaultfloat
+                  << diff << ", update: " << passes << "\n";
+        global_error = rmse;
+        if (diff <= o.tm_error || (passes >= mini_stop_passes && rmse <= o.tm_value)) {
+          std::cerr << "M: send terimination signal\n";
+          finished = true;
+          break;
+        }
+      }
+      if (checkpointing && now - last_cp >= o.cpinterval) {
+        const auto c0 = std::chrono::steady_clock::now();
+        const std::string f = cp_file(cp_epoch);
+        rc = nomad_gpu_save_checkpoint(ctx, f.c_str());
+        if (rc) {
+          std::cerr << "error in writing checkpoint " << f << ": " << nomad_gpu_last_error() << "\n";
+          break;
+        }
+        cp_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - c0).count();
+        last_cp = elapsed();
+        ++cp_epoch;
+        ++cp_count;
+      }
     }
     const auto t1 = std::chrono::steady_clock::now();
     train_time += std::chrono::duration<double>(t1 - t0).count();
@@ -294,17 +368,29 @@ int main(int argc, char** argv) {
     rc = nomad_gpu_sse(ctx, &s_tr, &c_tr, &s_te, &c_te);
     test_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
     if (rc) break;
-    // NomadBody::run statistics block (nb_main.cpp:267-285)
+    // NomadBody::run statistics block (nb_main.cpp:267-299)
     std::ostringstream buf;
     buf << "Statistics:\n"
         << "=====================================================\n";
-    buf << "elapsed time: " << o.timeouts[it] << " total training time: " << train_time
+    buf << "elapsed time: " << (finished ? train_time : o.timeouts[it]) << " total training time: " << train_time
         << " total testing time: " << test_time;
     buf << " current training RMSE: " << std::fixed << std::setprecision(10) << std::sqrt(s_tr / c_tr) << "\n";
     buf << "current test RMSE: " << std::fixed << std::setprecision(10) << std::sqrt(s_te / c_te) << "\n";
     buf << std::fixed << std::setprecision(4) << "detail: "
         << "train: s=" << s_tr << ", c=" << c_tr << "; test: s=" << s_te << ", c=" << c_te
         << "; u=" << updates << ", f=" << failures << ", s=" << sends << "\n";
+    if (checkpointing) {
+      // one writer: the master's and the workers' times are the same figure; no column
+      // message is in flight between epochs, so none is archived
+      const double each = cp_count ? cp_time / cp_count : 0.0;
+      buf << std::defaultfloat << "Number of checkpoints: " << cp_count << " Total time by master: " << cp_time
+          << " by worker: " << cp_time << " each one: " << each << "\n";
+      buf << "Total checkpoint writing time: " << cp_time << " each one: " << each
+          << " average on worker: " << each << "\n";
+      buf << "Number of archived message in each checkpoint:";
+      for (int i = 0; i < cp_count; ++i) buf << " 0";
+      buf << "\n";
+    }
     buf << "=====================================================";
     std::cout << buf.str() << std::endl;
     if (o.pause) std::this_thread::sleep_for(std::chrono::duration<double>(3.0));

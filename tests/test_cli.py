@@ -35,6 +35,17 @@ def test_bad_value_and_unknown_option(ng):
     assert r.returncode == 1 and "checkpoint type is inalid." in r.stderr
 
 
+def test_checkpoint_options_are_validated(ng):
+    """nomad_option.cpp:100-111: a checkpoint type needs a positive interval and a path."""
+    r = run("--path", "x", "--cptype", "sync")
+    assert r.returncode == 1 and "checkpoint interval is invalid." in r.stderr
+    r = run("--path", "x", "--cptype", "SYNC", "-k", "2")
+    assert r.returncode == 1 and "checkpoint path is not given." in r.stderr
+    for flag in ("--tm_value", "--tm_error", "--tm_interval", "--cpinterval", "--cppath",
+                 "--recover"):
+        assert flag in run("--help").stderr
+
+
 def test_unreadable_data_exits_11(ng, tmp_path):
     r = run("--path", str(tmp_path))
     assert r.returncode == 11 and "error in reading training file" in r.stderr
@@ -75,3 +86,65 @@ def test_epochs_and_modes(ng, gpu_ok, tmp_path):
         assert r.returncode == 0, (mode, r.stderr)
         rm = float(re.findall(r"current test RMSE: ([0-9.]+)", r.stdout)[0])
         assert np.isfinite(rm)
+
+
+def _stats(out):
+    return re.findall(r"detail: train: s=([0-9.]+), c=(\d+); test: s=([0-9.]+), c=(\d+); "
+                      r"u=(\d+), f=(\d+), s=(\d+)", out)
+
+
+@pytest.mark.gpu
+def test_termination_on_small_change(ng, gpu_ok, tmp_path):
+    """nb_master.cpp:21-23: the first check always continues (the previous RMSE is
+    infinite); a tolerance above any change stops training at the second check, and the
+    run ends after one statistics block although more timeout points are listed."""
+    tr, _ = _write_dataset(ng, str(tmp_path))
+    r = run("--path", str(tmp_path), "--dim", "8", "--lrate", "0.01", "--reg", "0.05",
+            "--epochs", "50", "--timeout", "1", "2", "--pause", "0", "--mode", "replay",
+            "--tm_interval", "0", "--tm_error", "1e9")
+    assert r.returncode == 0, r.stderr
+    st = _stats(r.stdout)
+    assert len(st) == 1 and int(st[0][4]) == 2 * tr.nnz
+    assert r.stderr.count("M: termination check at") == 2
+    assert "M: send terimination signal" in r.stderr
+
+
+@pytest.mark.gpu
+def test_termination_on_value_after_eight_passes(ng, gpu_ok, tmp_path):
+    """The value condition stops training only once every column made 8 passes."""
+    tr, _ = _write_dataset(ng, str(tmp_path))
+    r = run("--path", str(tmp_path), "--dim", "8", "--lrate", "0.01", "--reg", "0.05",
+            "--epochs", "50", "--pause", "0", "--mode", "replay", "--tm_interval", "0",
+            "--tm_error", "0", "--tm_value", "100")
+    assert r.returncode == 0, r.stderr
+    st = _stats(r.stdout)
+    assert len(st) == 1 and int(st[0][4]) == 8 * tr.nnz
+    rm = [float(x) for x in re.findall(r"RMSE: ([0-9.]+), difference", r.stderr)]
+    assert len(rm) == 8 and all(np.isfinite(rm))
+
+
+@pytest.mark.gpu
+def test_checkpoint_and_recover(ng, gpu_ok, tmp_path):
+    """--cptype sync writes cp-t<jobid>-e<k>.ckpt between epochs; --recover k resumes, and
+    in replay mode 2 epochs + recover + 1 epoch dumps the same factors as 3 epochs."""
+    data, cp = tmp_path / "data", tmp_path / "cp"
+    data.mkdir()
+    cp.mkdir()
+    _write_dataset(ng, str(data))
+    common = ("--path", str(data), "--dim", "8", "--lrate", "0.01", "--reg", "0.05",
+              "--pause", "0", "--mode", "replay", "--tm_interval", "1e9")
+    r = run(*common, "--epochs", "2", "--cptype", "sync", "--cpinterval", "1e-9",
+            "--cppath", str(cp), "--jobid", "7")
+    assert r.returncode == 0, r.stderr
+    assert "Number of checkpoints: 2 " in r.stdout
+    assert "Number of archived message in each checkpoint: 0 0" in r.stdout
+    assert sorted(os.listdir(cp)) == ["cp-t7-e0.ckpt", "cp-t7-e1.ckpt"]
+    assert ng.read_checkpoint(str(cp / "cp-t7-e1.ckpt"))[2] == 2
+    r1 = run(*common, "--epochs", "1", "--recover", "1", "--cppath", str(cp), "--jobid", "7",
+             "--output", str(tmp_path / "resumed"))
+    assert r1.returncode == 0, r1.stderr
+    r2 = run(*common, "--epochs", "3", "--output", str(tmp_path / "straight"))
+    assert r2.returncode == 0, r2.stderr
+    assert open(tmp_path / "resumed0").read() == open(tmp_path / "straight0").read()
+    r3 = run(*common, "--epochs", "1", "--recover", "5", "--cppath", str(cp), "--jobid", "7")
+    assert r3.returncode == 1 and "error in restoring checkpoint" in r3.stderr

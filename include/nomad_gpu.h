@@ -53,7 +53,15 @@ enum nomad_gpu_status {
 enum nomad_gpu_mode {
   NOMAD_MODE_ASYNC = 0,  /* NOMAD: worker warps pass column tokens through queues */
   NOMAD_MODE_DSGD = 1,   /* DSGD stratum sweep (Code/competitor/sgd-mpi-omp.cpp)  */
-  NOMAD_MODE_REPLAY = 2  /* one worker, columns round-robin: deterministic order  */
+  NOMAD_MODE_REPLAY = 2, /* one worker, columns round-robin: deterministic order  */
+  NOMAD_MODE_DSGDPP = 3  /* DSGD++ (Code/competitor/dsgdpp.cpp): innerB row blocks x
+                            2*innerB column blocks, two column halves per pass     */
+};
+enum nomad_gpu_lr_strategy {
+  NOMAD_LR_FIXED = 0,      /* step = lrate*1.5/(1 + drate*pass^1.5)                 */
+  NOMAD_LR_BOLD_DRIVER = 1 /* DSGD / DSGD++: after each pass the objective is
+                              recomputed; lr *= drate if it rose, else lr *= 1.05
+                              (sgd-mpi-omp.cpp:384-394, dsgdpp.cpp:512-521)         */
 };
 enum nomad_gpu_precision {
   NOMAD_PREC_FP32 = 0,   /* W, H stored in fp32                                   */
@@ -93,7 +101,8 @@ typedef struct nomad_gpu_params {
   int32_t priority_permille; /* ASYNC: columns with at least this many permille of the
                           largest column's ratings use the workers' priority queues;
                           0 = default 50, negative = no priority queue                */
-  int32_t reserved[6];
+  int32_t lr_strategy; /* nomad_gpu_lr_strategy (BOLD_DRIVER: DSGD and DSGDPP)  FIXED */
+  int32_t reserved[5];
 } nomad_gpu_params;
 
 /* One rating set in either the reference's row-major file layout (row_counts !=
@@ -126,6 +135,8 @@ typedef struct nomad_gpu_epoch_stats {
   double device_ms;    /* CUDA-event time of the call's device work on its stream  */
   double host_seconds; /* wall time of the call                                    */
   double online_sse;   /* sum of e^2 seen while training (ColumnData::error)       */
+  double objective;    /* BOLD_DRIVER: objective after the call (calobj_mpi), else 0 */
+  double lrate;        /* BOLD_DRIVER: learning rate of the next pass, else 0      */
 } nomad_gpu_epoch_stats;
 
 typedef struct nomad_gpu_info {
@@ -179,20 +190,29 @@ int nomad_gpu_set_factors(nomad_gpu_ctx* ctx, const float* W, const float* H);
 
 /* Set the cumulative pass count, the quantity the step size of the next epoch is
  * computed from (nb_main.cpp:514-515): the next nomad_gpu_epoch runs pass
- * epochs_done + 1.  Used when training resumes from saved factors. */
+ * epochs_done + 1.  Used when training resumes from saved factors.  Under the bold
+ * driver the learning rate and the last objective are the rest of the state; a
+ * checkpoint carries them. */
 int nomad_gpu_set_epochs_done(nomad_gpu_ctx* ctx, int32_t epochs_done);
 
-/* Write the context's factors and pass count to a checkpoint file (the format of
- * nomad_io_write_checkpoint).  Between nomad_gpu_epoch calls every column token has
- * finished its pass, so this is the whole training state.  BF16 factors are widened
- * to fp32 exactly. */
+/* Write the context's factors, pass count and bold-driver state to a checkpoint file
+ * (the format of nomad_io_write_checkpoint).  Between nomad_gpu_epoch calls every
+ * column token has finished its pass, so this is the whole training state.  BF16
+ * factors are widened to fp32 exactly. */
 int nomad_gpu_save_checkpoint(nomad_gpu_ctx* ctx, const char* path);
 
-/* Restore factors and pass count from a checkpoint file written for a problem of the
- * same m, n and dim (NOMAD_ERR_INVALID_ARG otherwise).  A REPLAY or DSGD context
- * restored from the checkpoint of epoch k and run for e epochs ends with the same
- * factors, bit for bit, as one that ran k + e epochs without stopping. */
+/* Restore factors, pass count and bold-driver state from a checkpoint file written
+ * for a problem of the same m, n and dim (NOMAD_ERR_INVALID_ARG otherwise).  A
+ * REPLAY, DSGD or DSGDPP context restored from the checkpoint of epoch k and run for
+ * e epochs ends with the same factors, bit for bit, as one that ran k + e epochs
+ * without stopping. */
 int nomad_gpu_load_checkpoint(nomad_gpu_ctx* ctx, const char* path);
+
+/* The DSGD objective of the current factors (calobj_mpi, sgd-mpi-omp.cpp:122-160):
+ * sum over training ratings of e^2 + reg * (sum_i nnz_row(i) |w_i|^2 +
+ * sum_j nnz_col(j) |h_j|^2), e in fp32 as in nomad_gpu_sse, everything summed in
+ * FP64.  Any mode.  The first call counts the ratings of every row on the device. */
+int nomad_gpu_objective(nomad_gpu_ctx* ctx, double* objective);
 
 /* Describe the context (sizes, workers, segments, memory). */
 int nomad_gpu_get_info(nomad_gpu_ctx* ctx, nomad_gpu_info* info);

@@ -69,29 +69,38 @@ int nomad_io_write_factors(const char* path, int32_t m, int32_t n, int32_t dim,
                            const float* W, const float* H);
 
 /* Checkpoint file: the whole training state at an epoch boundary, where every column
- * token has finished its pass, so no token is in flight and the factors plus the pass
- * count are all there is to keep (the reference also archives the column messages
- * queued at the cut, nb_checkpoint.cpp:61-102; at an epoch boundary there are none).
+ * token has finished its pass, so no token is in flight and the factors, the pass
+ * count and (bold driver) the learning rate and last objective are all there is to
+ * keep (the reference also archives the column messages queued at the cut,
+ * nb_checkpoint.cpp:61-102; at an epoch boundary there are none).
  * Layout, little-endian:
  *   char     magic[8] = "NOMADCP1"
  *   int32    m, n, dim, epochs_done
- *   uint64   FNV-1a 64 hash of the W and H bytes that follow
+ *   float64  lrate, objective      (0 and -1 when no bold-driver state is kept)
+ *   uint64   FNV-1a 64 hash of the 32 bytes of sizes, pass count, lrate and
+ *            objective above, continued over the W and H bytes that follow
  *   float32  W[m * dim], H[n * dim]   (row-major)
  * The file is written under path + ".tmp" and renamed over path, so a crash while
  * writing leaves an existing checkpoint at path intact. */
-int nomad_io_write_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim,
-                              int32_t epochs_done, const float* W, const float* H);
+typedef struct nomad_io_checkpoint_info {
+  int32_t m, n, dim, epochs_done;
+  double lrate;      /* bold driver: learning rate of the next pass; 0: none       */
+  double objective;  /* bold driver: objective after the last pass; < 0: none      */
+} nomad_io_checkpoint_info;
 
-/* Sizes and pass count of a checkpoint file (any output may be NULL).
- * NOMAD_ERR_FORMAT when the magic or the sizes are wrong. */
-int nomad_io_read_checkpoint_header(const char* path, int32_t* m, int32_t* n, int32_t* dim,
-                                    int32_t* epochs_done);
+int nomad_io_write_checkpoint(const char* path, const nomad_io_checkpoint_info* info,
+                              const float* W, const float* H);
+
+/* Header of a checkpoint file.  NOMAD_ERR_FORMAT when the magic or the sizes are
+ * wrong. */
+int nomad_io_read_checkpoint_header(const char* path, nomad_io_checkpoint_info* info);
 
 /* Read a checkpoint whose sizes must equal m, n, dim (else NOMAD_ERR_INVALID_ARG).
  * NOMAD_ERR_FORMAT when the file is short, longer than its sizes say, or its hash
- * does not match.  W or H may be NULL to skip it (the hash is still checked). */
+ * does not match.  W or H may be NULL to skip it (the hash is still checked); info
+ * may be NULL. */
 int nomad_io_read_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim,
-                             float* W, float* H, int32_t* epochs_done);
+                             float* W, float* H, nomad_io_checkpoint_info* info);
 
 /* The reference's initial factors, single rank: rows in init_parts blocks of
  * ceil(m/init_parts), block t drawn from mt19937_64(seed + t + 1); columns from

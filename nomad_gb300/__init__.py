@@ -18,7 +18,9 @@ import numpy as np
 from . import _abi
 from ._abi import NomadError, check, lib  # noqa: F401
 
-MODES = {"async": _abi.MODE_ASYNC, "dsgd": _abi.MODE_DSGD, "replay": _abi.MODE_REPLAY}
+MODES = {"async": _abi.MODE_ASYNC, "dsgd": _abi.MODE_DSGD, "replay": _abi.MODE_REPLAY,
+         "dsgdpp": _abi.MODE_DSGDPP}
+LR_STRATEGIES = {"fixed": _abi.LR_FIXED, "bold": _abi.LR_BOLD_DRIVER}
 PRECISIONS = {"fp32": _abi.PREC_FP32, "bf16": _abi.PREC_BF16_SR}
 INITS = {"reference": _abi.INIT_REFERENCE, "hash": _abi.INIT_HASH}
 
@@ -152,26 +154,28 @@ def write_factors(path, W, H):
                                        _ptr(W), _ptr(H)), "nomad_io_write_factors")
 
 
-def write_checkpoint(path, W, H, epochs_done):
-    """Checkpoint file of factors W[m,dim], H[n,dim] after `epochs_done` passes."""
+def write_checkpoint(path, W, H, epochs_done, lrate=0.0, objective=-1.0):
+    """Checkpoint file of factors W[m,dim], H[n,dim] after `epochs_done` passes, with
+    the bold driver's learning rate and last objective (0 and -1: none)."""
     W = np.ascontiguousarray(W, np.float32)
     H = np.ascontiguousarray(H, np.float32)
-    check(lib().nomad_io_write_checkpoint(os.fsencode(path), W.shape[0], H.shape[0], W.shape[1],
-                                          epochs_done, _ptr(W), _ptr(H)),
+    info = _abi.CheckpointInfo(W.shape[0], H.shape[0], W.shape[1], epochs_done, lrate, objective)
+    check(lib().nomad_io_write_checkpoint(os.fsencode(path), ctypes.byref(info), _ptr(W), _ptr(H)),
           "nomad_io_write_checkpoint")
 
 
-def read_checkpoint(path):
-    """(W, H, epochs_done) from a checkpoint file."""
-    m, n, dim, ep = (ctypes.c_int32() for _ in range(4))
-    check(lib().nomad_io_read_checkpoint_header(os.fsencode(path), ctypes.byref(m), ctypes.byref(n),
-                                                ctypes.byref(dim), ctypes.byref(ep)),
+def read_checkpoint(path, with_info=False):
+    """(W, H, epochs_done) from a checkpoint file; with_info: (W, H, info dict)."""
+    info = _abi.CheckpointInfo()
+    check(lib().nomad_io_read_checkpoint_header(os.fsencode(path), ctypes.byref(info)),
           "nomad_io_read_checkpoint_header")
-    W = np.empty((m.value, dim.value), np.float32)
-    H = np.empty((n.value, dim.value), np.float32)
-    check(lib().nomad_io_read_checkpoint(os.fsencode(path), m.value, n.value, dim.value, _ptr(W),
-                                         _ptr(H), ctypes.byref(ep)), "nomad_io_read_checkpoint")
-    return W, H, ep.value
+    W = np.empty((info.m, info.dim), np.float32)
+    H = np.empty((info.n, info.dim), np.float32)
+    check(lib().nomad_io_read_checkpoint(os.fsencode(path), info.m, info.n, info.dim, _ptr(W),
+                                         _ptr(H), ctypes.byref(info)), "nomad_io_read_checkpoint")
+    if with_info:
+        return W, H, {k: getattr(info, k) for k, _ in _abi.CheckpointInfo._fields_}
+    return W, H, info.epochs_done
 
 
 def default_params(**overrides):
@@ -184,6 +188,8 @@ def default_params(**overrides):
             v = PRECISIONS[v] if isinstance(v, str) else v
         elif k == "init":
             v = INITS[v] if isinstance(v, str) else v
+        elif k == "lr_strategy":
+            v = LR_STRATEGIES[v] if isinstance(v, str) else v
         setattr(p, k, v)
     return p
 
@@ -239,6 +245,12 @@ class Nomad:
         W = None if W is None else np.ascontiguousarray(W, np.float32)
         H = None if H is None else np.ascontiguousarray(H, np.float32)
         check(lib().nomad_gpu_set_factors(self._ctx, _ptr(W), _ptr(H)), "nomad_gpu_set_factors")
+
+    def objective(self):
+        """calobj_mpi of the current factors: SSE + reg * weighted squared norms."""
+        o = ctypes.c_double()
+        check(lib().nomad_gpu_objective(self._ctx, ctypes.byref(o)), "nomad_gpu_objective")
+        return o.value
 
     def set_epochs_done(self, epochs_done):
         check(lib().nomad_gpu_set_epochs_done(self._ctx, epochs_done), "nomad_gpu_set_epochs_done")

@@ -27,7 +27,8 @@ ERR_FORMAT = -7
 ERR_NO_DEVICE = -8
 ERR_UNSUPPORTED = -9
 
-MODE_ASYNC, MODE_DSGD, MODE_REPLAY = 0, 1, 2
+MODE_ASYNC, MODE_DSGD, MODE_REPLAY, MODE_DSGDPP = 0, 1, 2, 3
+LR_FIXED, LR_BOLD_DRIVER = 0, 1
 PREC_FP32, PREC_BF16_SR = 0, 1
 INIT_REFERENCE, INIT_HASH = 0, 1
 FILE_ID_INT, FILE_ID_LONG = 1211216, 1015
@@ -43,7 +44,7 @@ class Params(ctypes.Structure):
                 ("warps_per_block", c_i32), ("blocks_per_sm", c_i32), ("balance", c_i32),
                 ("dsgd_inner_blocks", c_i32), ("dsgd_strategy", c_i32), ("exact", c_i32),
                 ("spin_budget_ms", c_i32), ("debug_flags", c_i32), ("long_visit", c_i32),
-                ("priority_permille", c_i32), ("reserved", c_i32 * 6)]
+                ("priority_permille", c_i32), ("lr_strategy", c_i32), ("reserved", c_i32 * 5)]
 
 
 class Matrix(ctypes.Structure):
@@ -64,7 +65,13 @@ class BatchProblem(ctypes.Structure):
 class EpochStats(ctypes.Structure):
     _fields_ = [("updates", c_i64), ("hops", c_i64), ("failures", c_i64),
                 ("epochs_done", c_i32), ("reserved0", c_i32), ("device_ms", c_dbl),
-                ("host_seconds", c_dbl), ("online_sse", c_dbl)]
+                ("host_seconds", c_dbl), ("online_sse", c_dbl), ("objective", c_dbl),
+                ("lrate", c_dbl)]
+
+
+class CheckpointInfo(ctypes.Structure):
+    _fields_ = [("m", c_i32), ("n", c_i32), ("dim", c_i32), ("epochs_done", c_i32),
+                ("lrate", c_dbl), ("objective", c_dbl)]
 
 
 class Info(ctypes.Structure):
@@ -106,6 +113,7 @@ SIGNATURES = {
     "nomad_gpu_set_factors": (ctypes.c_int, [c_vp, c_vp, c_vp]),
     "nomad_gpu_get_info": (ctypes.c_int, [c_vp, ctypes.POINTER(Info)]),
     "nomad_gpu_set_epochs_done": (ctypes.c_int, [c_vp, c_i32]),
+    "nomad_gpu_objective": (ctypes.c_int, [c_vp, ctypes.POINTER(c_dbl)]),
     "nomad_gpu_save_checkpoint": (ctypes.c_int, [c_vp, ctypes.c_char_p]),
     "nomad_gpu_load_checkpoint": (ctypes.c_int, [c_vp, ctypes.c_char_p]),
     "nomad_gpu_destroy": (None, [c_vp]),
@@ -132,13 +140,12 @@ SIGNATURES = {
     "nomad_io_free": (None, [ctypes.POINTER(IoMatrix)]),
     "nomad_io_write_factors": (ctypes.c_int, [ctypes.c_char_p, c_i32, c_i32, c_i32, c_vp,
                                               c_vp]),
-    "nomad_io_write_checkpoint": (ctypes.c_int, [ctypes.c_char_p, c_i32, c_i32, c_i32, c_i32,
+    "nomad_io_write_checkpoint": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CheckpointInfo),
                                                  c_vp, c_vp]),
-    "nomad_io_read_checkpoint_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_i32),
-                                                       ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
-                                                       ctypes.POINTER(c_i32)]),
+    "nomad_io_read_checkpoint_header": (ctypes.c_int, [ctypes.c_char_p,
+                                                       ctypes.POINTER(CheckpointInfo)]),
     "nomad_io_read_checkpoint": (ctypes.c_int, [ctypes.c_char_p, c_i32, c_i32, c_i32, c_vp, c_vp,
-                                                ctypes.POINTER(c_i32)]),
+                                                ctypes.POINTER(CheckpointInfo)]),
     "nomad_reference_init": (ctypes.c_int, [c_i32, c_i32, c_i32, c_u64, c_i32, c_vp, c_vp]),
     "nomad_synth_preset": (ctypes.c_int, [c_i32, ctypes.POINTER(SynthSpec)]),
     "nomad_synth_generate": (ctypes.c_int, [ctypes.POINTER(SynthSpec),

@@ -58,7 +58,11 @@ struct nomad_gpu_ctx {
   int4* rates = nullptr;
   int64_t* blk_ptr = nullptr;
   int32_t* sched = nullptr;
-  int32_t innerB = 0;
+  int32_t innerB = 0, col_blocks = 0;
+  // bold driver (DSGD, DSGD++): learning rate of the next pass, objective after the
+  // last one (< 0: not computed yet)
+  double cur_lr = 0, last_obj = -1;
+  int32_t* row_nnz = nullptr;  // ratings per row, for the objective (lazily counted)
   // step sizes per pass count
   float* steps = nullptr;
   int32_t n_steps = 0;
@@ -342,13 +346,14 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     RC(dalloc(c, &c->stats, 4));
     RC(dalloc(c, &c->err_sum, 1));
     RC(reset_tokens(c));
-  } else if (p.mode == NOMAD_MODE_DSGD) {
+  } else if (p.mode == NOMAD_MODE_DSGD || p.mode == NOMAD_MODE_DSGDPP) {
     c->innerB = p.dsgd_inner_blocks > 0 ? p.dsgd_inner_blocks : 2 * c->num_sms * 4;
+    c->col_blocks = p.mode == NOMAD_MODE_DSGDPP ? 2 * c->innerB : c->innerB;
     nomad::DsgdLayout D;
-    RC(nomad::build_dsgd_layout(prob->train, f.m, f.n, c->innerB, D));
+    RC(nomad::build_dsgd_layout(prob->train, f.m, f.n, c->innerB, c->col_blocks, D));
     RC(upload(c, &c->blk_ptr, D.blk_ptr.data(), D.blk_ptr.size()));
     RC(upload(c, &c->rates, reinterpret_cast<const int4*>(D.rates.data()), D.rates.size() / 4));
-    RC(dalloc(c, &c->sched, static_cast<size_t>(c->innerB) * c->innerB));
+    RC(dalloc(c, &c->sched, static_cast<size_t>(c->col_blocks) * c->innerB));
   } else if (p.mode == NOMAD_MODE_REPLAY) {
     c->P = 1;
   } else {
@@ -357,7 +362,8 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   if (!c->err_sum) RC(dalloc(c, &c->err_sum, 1));
   c->sse_grid = c->num_sms * 8;
   RC(dalloc(c, &c->partials, c->sse_grid));
-  RC(dalloc(c, &c->sse_out, 2));
+  RC(dalloc(c, &c->sse_out, 5));  // train, test, objective: SSE, |W|, |H| terms
+  c->cur_lr = p.lrate;
   RC(ensure_steps(c, 64));
   CK(cudaStreamSynchronize(c->stream));
   return NOMAD_OK;
@@ -489,37 +495,92 @@ int epoch_replay(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   return NOMAD_OK;
 }
 
+// The DSGD objective (calobj_mpi, sgd-mpi-omp.cpp:122-160): training SSE plus
+// reg * (sum_i nnz_row(i) |w_i|^2 + sum_j nnz_col(j) |h_j|^2), all sums in FP64.
+int objective(nomad_gpu_ctx* c, double* obj) {
+  if (!c->row_nnz) {
+    RC(dalloc(c, &c->row_nnz, c->f.m));
+    CK(nomad::launch_count_rows(c->train, c->nnz_train, c->row_nnz, c->f.m, c->stream));
+  }
+  nomad::SseArgs a;
+  a.f = c->f;
+  a.partials = c->partials;
+  a.grid = c->sse_grid;
+  a.ratings = c->train;
+  a.col_ptr = c->train_ptr;
+  a.nnz = c->nnz_train;
+  a.out = c->sse_out + 2;
+  CK(nomad::launch_sse(a, c->stream));
+  // the kernels share the partials scratch; stream order keeps them apart
+  CK(nomad::launch_weighted_norm(c->f, true, c->row_nnz, nullptr, c->partials, c->sse_grid, c->sse_out + 3,
+                                 c->stream));
+  CK(nomad::launch_weighted_norm(c->f, false, nullptr, c->train_ptr, c->partials, c->sse_grid, c->sse_out + 4,
+                                 c->stream));
+  double h[3];
+  CK(cudaMemcpyAsync(h, c->sse_out + 2, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->d2h_bytes += static_cast<int64_t>(sizeof(h));
+  *obj = h[0] + c->prm.reg * (h[1] + h[2]);
+  return NOMAD_OK;
+}
+
+// DSGD (sgd-mpi-omp.cpp:220-424) and DSGD++ (dsgdpp.cpp:300-540), one process:
+// every pass runs its strata one launch after another (innerB strata for DSGD;
+// 2*innerB for DSGD++, the first innerB over the left column half, the rest over the
+// right half).  FIXED: step = 1.5*lrate/(1 + drate*iter^1.5) (sgd-mpi-omp.cpp:308-309,
+// dsgdpp.cpp:358-359).  BOLD_DRIVER: the step is the running learning rate; after the
+// pass the objective is recomputed and the rate multiplied by drate if the objective
+// rose, else by 1.05 (sgd-mpi-omp.cpp:384-394, dsgdpp.cpp:512-521); the objective of
+// the starting factors is computed once, before the first pass.
 int epoch_dsgd(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
+  const bool pp = c->prm.mode == NOMAD_MODE_DSGDPP;
+  const bool bold = c->prm.lr_strategy == NOMAD_LR_BOLD_DRIVER;
   nomad::DsgdArgs a;
   a.f = c->f;
   a.rates = c->rates;
   a.blk_ptr = c->blk_ptr;
   a.sched = c->sched;
   a.innerB = c->innerB;
+  a.col_blocks = c->col_blocks;
   a.lambda = static_cast<float>(c->prm.reg);
   a.seed32 = static_cast<uint32_t>(c->prm.seed ^ (c->prm.seed >> 32));
   a.exact = c->prm.exact;
+  const int32_t strata = pp ? 2 * c->innerB : c->innerB;
   std::vector<int32_t> sched;
   float total_ms = 0;
+  if (bold && c->last_obj < 0) RC(objective(c, &c->last_obj));
   for (int32_t k = 0; k < E; ++k) {
     const int32_t iter = c->epochs_done + k + 1;
-    nomad::dsgd_schedule(c->innerB, iter, c->prm.dsgd_strategy, sched);
+    if (pp)
+      nomad::dsgdpp_schedule(c->innerB, iter, c->prm.dsgd_strategy, sched);
+    else
+      nomad::dsgd_schedule(c->innerB, iter, c->prm.dsgd_strategy, sched);
     CK(cudaMemcpyAsync(c->sched, sched.data(), sched.size() * sizeof(int32_t),
                        cudaMemcpyHostToDevice, c->stream));
-    // FIXED schedule of dsgd_mpi (sgd-mpi-omp.cpp:308-309), lrate/decay in double
-    a.step = static_cast<float>(1.5 * c->prm.lrate / (1.0 + c->prm.drate * std::pow(iter, 1.5)));
+    a.step = bold ? static_cast<float>(c->cur_lr)
+                  : static_cast<float>(1.5 * c->prm.lrate / (1.0 + c->prm.drate * std::pow(iter, 1.5)));
     a.iter = iter;
     CK(cudaEventRecord(c->ev0, c->stream));
-    for (int32_t s = 0; s < c->innerB; ++s) CK(nomad::launch_dsgd_stratum(a, s, c->stream));
+    for (int32_t s = 0; s < strata; ++s) CK(nomad::launch_dsgd_stratum(a, s, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     total_ms += ms;
+    if (bold) {
+      double obj = 0;
+      RC(objective(c, &obj));
+      c->cur_lr *= obj > c->last_obj ? c->prm.drate : 1.05;
+      c->last_obj = obj;
+    }
   }
   if (st) {
     st->updates = c->nnz_train * E;
     st->device_ms = total_ms;
+    if (bold) {
+      st->objective = c->last_obj;
+      st->lrate = c->cur_lr;
+    }
   }
   return NOMAD_OK;
 }
@@ -562,6 +623,11 @@ int nomad_gpu_init(nomad_gpu_ctx** out, const nomad_gpu_problem* prob,
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown precision %d", params->precision);
   if (!(params->lrate >= 0) || !(params->drate >= 0) || !(params->reg >= 0))
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "lrate, drate and reg must be non-negative");
+  if (params->lr_strategy != NOMAD_LR_FIXED && params->lr_strategy != NOMAD_LR_BOLD_DRIVER)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown lr_strategy %d", params->lr_strategy);
+  if (params->lr_strategy == NOMAD_LR_BOLD_DRIVER && params->mode != NOMAD_MODE_DSGD &&
+      params->mode != NOMAD_MODE_DSGDPP)
+    NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "the bold driver is a DSGD / DSGD++ learning-rate strategy");
   std::unique_ptr<nomad_gpu_ctx> c(new nomad_gpu_ctx());
   c->prm = *params;
   if (c->prm.mode == NOMAD_MODE_REPLAY) c->prm.exact = 1;
@@ -669,22 +735,40 @@ int nomad_gpu_set_epochs_done(nomad_gpu_ctx* c, int32_t epochs_done) {
   return NOMAD_OK;
 }
 
+int nomad_gpu_objective(nomad_gpu_ctx* c, double* obj) {
+  nomad::clear_last_error();
+  if (!c || !obj) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
+  CK(cudaSetDevice(c->device));
+  return objective(c, obj);
+}
+
 int nomad_gpu_save_checkpoint(nomad_gpu_ctx* c, const char* path) {
   nomad::clear_last_error();
   if (!c || !path) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
   std::vector<float> W(static_cast<size_t>(c->f.m) * c->f.dim), H(static_cast<size_t>(c->f.n) * c->f.dim);
   RC(nomad_gpu_get_factors(c, W.data(), H.data()));
-  return nomad_io_write_checkpoint(path, c->f.m, c->f.n, c->f.dim, c->epochs_done, W.data(), H.data());
+  nomad_io_checkpoint_info info{c->f.m, c->f.n, c->f.dim, c->epochs_done, 0.0, -1.0};
+  if (c->prm.lr_strategy == NOMAD_LR_BOLD_DRIVER) {
+    info.lrate = c->cur_lr;
+    info.objective = c->last_obj;
+  }
+  return nomad_io_write_checkpoint(path, &info, W.data(), H.data());
 }
 
 int nomad_gpu_load_checkpoint(nomad_gpu_ctx* c, const char* path) {
   nomad::clear_last_error();
   if (!c || !path) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
   std::vector<float> W(static_cast<size_t>(c->f.m) * c->f.dim), H(static_cast<size_t>(c->f.n) * c->f.dim);
-  int32_t ep = 0;
-  RC(nomad_io_read_checkpoint(path, c->f.m, c->f.n, c->f.dim, W.data(), H.data(), &ep));
+  nomad_io_checkpoint_info info;
+  RC(nomad_io_read_checkpoint(path, c->f.m, c->f.n, c->f.dim, W.data(), H.data(), &info));
+  if (c->prm.lr_strategy == NOMAD_LR_BOLD_DRIVER && info.lrate <= 0)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "checkpoint %s holds no bold-driver learning rate", path);
   RC(nomad_gpu_set_factors(c, W.data(), H.data()));
-  return nomad_gpu_set_epochs_done(c, ep);
+  if (c->prm.lr_strategy == NOMAD_LR_BOLD_DRIVER) {
+    c->cur_lr = info.lrate;
+    c->last_obj = info.objective;
+  }
+  return nomad_gpu_set_epochs_done(c, info.epochs_done);
 }
 
 int nomad_gpu_get_info(nomad_gpu_ctx* c, nomad_gpu_info* info) {

@@ -238,12 +238,12 @@ int nomad_reference_init(int32_t m, int32_t n, int32_t dim, uint64_t seed,
   return NOMAD_OK;
 }
 
-// Checkpoint file (own format): the factors and the pass count at an epoch boundary.
-// Plays the part of NomadBody::archive_local / restore_local (nb_checkpoint.cpp:47-59,
-// 114-120), which keep each worker thread's rows as doubles in a ".state" file.
+// Checkpoint file (own format): factors, pass count and bold-driver state at an
+// epoch boundary.  Plays the part of NomadBody::archive_local / restore_local
+// (nb_checkpoint.cpp:47-59, 114-120), which keep each worker thread's rows as
+// doubles in a ".state" file.
 namespace {
 constexpr char kCkptMagic[8] = {'N', 'O', 'M', 'A', 'D', 'C', 'P', '1'};
-constexpr int64_t kCkptHeader = 8 + 16 + 8;
 
 uint64_t fnv1a64(uint64_t h, const void* data, size_t bytes) {
   const unsigned char* p = static_cast<const unsigned char*>(data);
@@ -255,33 +255,51 @@ uint64_t fnv1a64(uint64_t h, const void* data, size_t bytes) {
 }
 constexpr uint64_t kFnvBasis = 14695981039346656037ULL;
 
-int ckpt_header(std::ifstream& f, const char* path, int32_t h[4], uint64_t* hash) {
+// header after the magic: int32 m, n, dim, epochs_done; float64 lrate, objective.
+// *fields_hash = FNV-1a 64 of those 32 bytes, the start of the file's hash.
+int ckpt_header(std::ifstream& f, const char* path, nomad_io_checkpoint_info* info, uint64_t* hash,
+                uint64_t* fields_hash) {
   char magic[8];
   if (!f.read(magic, 8) || std::memcmp(magic, kCkptMagic, 8) != 0)
     NOMAD_FAIL(NOMAD_ERR_FORMAT, "%s is not a checkpoint file", path);
-  if (!f.read(reinterpret_cast<char*>(h), 16) || !f.read(reinterpret_cast<char*>(hash), 8))
+  int32_t h[4];
+  double d[2];
+  if (!f.read(reinterpret_cast<char*>(h), 16) || !f.read(reinterpret_cast<char*>(d), 16) ||
+      !f.read(reinterpret_cast<char*>(hash), 8))
     NOMAD_FAIL(NOMAD_ERR_FORMAT, "short checkpoint header in %s", path);
   if (h[0] < 0 || h[1] < 0 || h[2] <= 0 || h[3] < 0)
     NOMAD_FAIL(NOMAD_ERR_FORMAT, "invalid sizes in checkpoint header of %s", path);
+  info->m = h[0];
+  info->n = h[1];
+  info->dim = h[2];
+  info->epochs_done = h[3];
+  info->lrate = d[0];
+  info->objective = d[1];
+  *fields_hash = fnv1a64(fnv1a64(kFnvBasis, h, sizeof(h)), d, sizeof(d));
   return NOMAD_OK;
 }
 }  // namespace
 
-int nomad_io_write_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim,
-                              int32_t epochs_done, const float* W, const float* H) {
+int nomad_io_write_checkpoint(const char* path, const nomad_io_checkpoint_info* info, const float* W,
+                              const float* H) {
   nomad::clear_last_error();
-  if (!path || m < 0 || n < 0 || dim <= 0 || epochs_done < 0 || (m > 0 && !W) || (n > 0 && !H))
+  if (!path || !info) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_io_write_checkpoint");
+  const int32_t m = info->m, n = info->n, dim = info->dim;
+  if (m < 0 || n < 0 || dim <= 0 || info->epochs_done < 0 || (m > 0 && !W) || (n > 0 && !H))
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_io_write_checkpoint");
   const size_t wb = static_cast<size_t>(m) * dim * sizeof(float);
   const size_t hb = static_cast<size_t>(n) * dim * sizeof(float);
-  uint64_t hash = fnv1a64(fnv1a64(kFnvBasis, W, m ? wb : 0), H, n ? hb : 0);
+  const int32_t h[4] = {m, n, dim, info->epochs_done};
+  const double d[2] = {info->lrate, info->objective};
+  uint64_t hash = fnv1a64(fnv1a64(kFnvBasis, h, sizeof(h)), d, sizeof(d));
+  hash = fnv1a64(fnv1a64(hash, W, m ? wb : 0), H, n ? hb : 0);
   const std::string tmp = std::string(path) + ".tmp";
   {
     std::ofstream f(tmp, std::ios::out | std::ios::binary | std::ios::trunc);
     if (!f) NOMAD_FAIL(NOMAD_ERR_IO, "cannot open %s for writing", tmp.c_str());
-    const int32_t h[4] = {m, n, dim, epochs_done};
     f.write(kCkptMagic, 8);
     f.write(reinterpret_cast<const char*>(h), sizeof(h));
+    f.write(reinterpret_cast<const char*>(d), sizeof(d));
     f.write(reinterpret_cast<const char*>(&hash), sizeof(hash));
     if (m) f.write(reinterpret_cast<const char*>(W), static_cast<std::streamsize>(wb));
     if (n) f.write(reinterpret_cast<const char*>(H), static_cast<std::streamsize>(hb));
@@ -298,39 +316,30 @@ int nomad_io_write_checkpoint(const char* path, int32_t m, int32_t n, int32_t di
   return NOMAD_OK;
 }
 
-int nomad_io_read_checkpoint_header(const char* path, int32_t* m, int32_t* n, int32_t* dim,
-                                    int32_t* epochs_done) {
+int nomad_io_read_checkpoint_header(const char* path, nomad_io_checkpoint_info* info) {
   nomad::clear_last_error();
-  if (!path) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null path");
+  if (!path || !info) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments");
   std::ifstream f(path, std::ios::in | std::ios::binary);
   if (!f) NOMAD_FAIL(NOMAD_ERR_IO, "cannot open file: %s", path);
-  int32_t h[4];
-  uint64_t hash = 0;
-  const int rc = ckpt_header(f, path, h, &hash);
-  if (rc) return rc;
-  if (m) *m = h[0];
-  if (n) *n = h[1];
-  if (dim) *dim = h[2];
-  if (epochs_done) *epochs_done = h[3];
-  return NOMAD_OK;
+  uint64_t hash = 0, fields = 0;
+  return ckpt_header(f, path, info, &hash, &fields);
 }
 
-int nomad_io_read_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim, float* W,
-                             float* H, int32_t* epochs_done) {
+int nomad_io_read_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim, float* W, float* H,
+                             nomad_io_checkpoint_info* info) {
   nomad::clear_last_error();
   if (!path || m < 0 || n < 0 || dim <= 0)
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_io_read_checkpoint");
   std::ifstream f(path, std::ios::in | std::ios::binary);
   if (!f) NOMAD_FAIL(NOMAD_ERR_IO, "cannot open file: %s", path);
-  int32_t h[4];
-  uint64_t want = 0;
-  const int rc = ckpt_header(f, path, h, &want);
+  nomad_io_checkpoint_info hdr;
+  uint64_t want = 0, hash = 0;
+  const int rc = ckpt_header(f, path, &hdr, &want, &hash);
   if (rc) return rc;
-  if (h[0] != m || h[1] != n || h[2] != dim)
+  if (hdr.m != m || hdr.n != n || hdr.dim != dim)
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "checkpoint %s holds m=%d n=%d dim=%d, expected m=%d n=%d dim=%d", path,
-               h[0], h[1], h[2], m, n, dim);
+               hdr.m, hdr.n, hdr.dim, m, n, dim);
   // Read in bounded chunks so that a NULL output still has its bytes hashed.
-  uint64_t hash = kFnvBasis;
   std::vector<char> buf;
   auto part = [&](float* out, int64_t count) -> bool {
     int64_t left = count * static_cast<int64_t>(sizeof(float));
@@ -351,7 +360,7 @@ int nomad_io_read_checkpoint(const char* path, int32_t m, int32_t n, int32_t dim
   if (f.peek() != std::char_traits<char>::eof())
     NOMAD_FAIL(NOMAD_ERR_FORMAT, "checkpoint %s is longer than its header says", path);
   if (hash != want) NOMAD_FAIL(NOMAD_ERR_FORMAT, "checkpoint %s fails its hash check", path);
-  if (epochs_done) *epochs_done = h[3];
+  if (info) *info = hdr;
   return NOMAD_OK;
 }
 

@@ -297,21 +297,22 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
 }
 
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
-                      DsgdLayout& D) {
+                      int32_t col_blocks, DsgdLayout& D) {
   RowMajor R;
   int rc = to_row_major(A, m, n, R);
   if (rc) return rc;
-  if (innerB <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "DSGD needs innerB > 0");
+  if (innerB <= 0 || col_blocks <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "DSGD needs innerB > 0");
   D.innerB = innerB;
+  D.col_blocks = col_blocks;
   D.innerBm = m / innerB + ((m % innerB) ? 1 : 0);
-  D.innerBn = n / innerB + ((n % innerB) ? 1 : 0);
+  D.innerBn = n / col_blocks + ((n % col_blocks) ? 1 : 0);
   if (D.innerBm == 0) D.innerBm = 1;
   if (D.innerBn == 0) D.innerBn = 1;
-  const int64_t nb = static_cast<int64_t>(innerB) * innerB;
+  const int64_t nb = static_cast<int64_t>(innerB) * col_blocks;
   const int64_t nnz = A.nnz;
   D.blk_ptr.assign(static_cast<size_t>(nb) + 1, 0);
   auto bid_of = [&](int32_t r, int32_t c) {
-    return static_cast<int64_t>(r / D.innerBm) * innerB + c / D.innerBn;
+    return static_cast<int64_t>(r / D.innerBm) * col_blocks + c / D.innerBn;
   };
   for (int32_t r = 0; r < m; ++r)
     for (int64_t i = R.row_ptr[r]; i < R.row_ptr[r + 1]; ++i) D.blk_ptr[bid_of(r, R.cols[i]) + 1]++;
@@ -358,6 +359,31 @@ void dsgd_schedule(int32_t innerB, int32_t iter, int32_t strategy, std::vector<i
     for (int32_t ii = 0; ii < innerB; ++ii) cur[perm[ii]] = (ii + offset[i]) % innerB;
     for (int32_t bi = 0; bi < innerB; ++bi) out[static_cast<size_t>(i) * innerB + bi] = cur[bi];
   }
+}
+
+void dsgdpp_schedule(int32_t innerB, int32_t iter, int32_t strategy, std::vector<int32_t>& out) {
+  // dsgd_mpi of dsgdpp.cpp resets inner_perm / inner_offset to the identity every
+  // iteration; under WOR_STRATUM they are shuffled once, in phase 0, after
+  // srand(34586 + iter) (the outer B = 1 shuffles draw nothing), and phase 1 reuses
+  // them.
+  std::vector<int32_t> perm(innerB), offset(innerB), cur(innerB);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::iota(offset.begin(), offset.end(), 0);
+  if (strategy == 2) {
+    GlibcRand g(34586u + static_cast<unsigned>(iter));
+    for (auto* a : {&perm, &offset})
+      for (size_t i = 1; i < a->size(); ++i) {
+        const size_t j = static_cast<size_t>(g.next()) % (i + 1);
+        if (i != j) std::swap((*a)[i], (*a)[j]);
+      }
+  }
+  out.assign(static_cast<size_t>(2) * innerB * innerB, 0);
+  for (int32_t p = 0; p < 2; ++p)
+    for (int32_t i = 0; i < innerB; ++i) {
+      for (int32_t ii = 0; ii < innerB; ++ii) cur[perm[ii]] = (ii + offset[i]) % innerB;
+      for (int32_t bi = 0; bi < innerB; ++bi)
+        out[(static_cast<size_t>(p) * innerB + i) * innerB + bi] = p * innerB + cur[bi];
+    }
 }
 
 }  // namespace nomad

@@ -2,6 +2,7 @@
 // initialisation and layout-conversion kernels for sm_103a.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "common.h"
@@ -114,6 +115,53 @@ __global__ void sum_partials_kernel(const double* __restrict__ partials, int cou
   if (threadIdx.x == 0) *out = red[0];
 }
 
+// Ratings per row of a CSC rating set (integer atomics: exact, order-free).
+__global__ void count_rows_kernel(const int2* __restrict__ ratings, int64_t nnz, int32_t* counts) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nnz;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    atomicAdd(&counts[__ldg(&ratings[i]).x], 1);
+}
+
+// Regulariser of the DSGD objective (calobj_mpi, sgd-mpi-omp.cpp:141-148): the sum
+// over rows r of count(r) * |x_r|^2, count(r) = counts[r] (rows of W) or
+// ptr[r+1] - ptr[r] (columns of H).  A warp takes a row, lanes across its elements;
+// squares of the stored values and every sum in FP64.  Each block writes one partial
+// in a fixed order.
+template <typename Store>
+__global__ void __launch_bounds__(256) weighted_norm_kernel(const Store* __restrict__ X, int64_t rows,
+                                                            int dim, int kpad, const int32_t* __restrict__ counts,
+                                                            const int64_t* __restrict__ ptr,
+                                                            double* __restrict__ partials) {
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int warps = blockDim.x >> 5;
+  double acc = 0.0;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * warps + wib; r < rows;
+       r += static_cast<int64_t>(gridDim.x) * warps) {
+    const int64_t cnt = counts ? static_cast<int64_t>(__ldg(&counts[r])) : __ldg(&ptr[r + 1]) - __ldg(&ptr[r]);
+    if (cnt == 0) continue;
+    double sq = 0.0;
+    for (int k = lane; k < dim; k += 32) {
+      float x;
+      if (sizeof(Store) == 4)
+        x = __ldg(reinterpret_cast<const float*>(X) + r * kpad + k);
+      else
+        x = __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(X)[r * kpad + k]);
+      sq += static_cast<double>(x) * static_cast<double>(x);
+    }
+    acc += static_cast<double>(cnt) * sq;
+  }
+  for (int s = 16; s >= 1; s >>= 1) acc += __shfl_xor_sync(kFull, acc, s);
+  __shared__ double red[32];
+  if (lane == 0) red[wib] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < warps; ++i) s += red[i];
+    partials[blockIdx.x] = s;
+  }
+}
+
 // U(0, 1/sqrt(dim)) factors from a counter hash of (seed, row, element); padding 0.
 template <typename Store>
 __global__ void init_hash_kernel(Store* __restrict__ X, int64_t rows, int dim, int kpad,
@@ -194,6 +242,31 @@ cudaError_t launch_sse(const SseArgs& a, cudaStream_t s) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   sum_partials_kernel<<<1, 256, 0, s>>>(a.partials, a.grid, a.out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_rows(const int2* ratings, int64_t nnz, int32_t* counts, int32_t m, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * std::max(m, 1), s);
+  if (e != cudaSuccess || nnz == 0) return e;
+  count_rows_kernel<<<grid_for(nnz), 256, 0, s>>>(ratings, nnz, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weighted_norm(const DevFactors& f, bool rows_of_w, const int32_t* counts,
+                                 const int64_t* ptr, double* partials, int32_t grid, double* out,
+                                 cudaStream_t s) {
+  const void* X = rows_of_w ? f.W : f.H;
+  const int64_t rows = rows_of_w ? f.m : f.n;
+  if (rows == 0) return cudaMemsetAsync(out, 0, sizeof(double), s);
+  if (f.bf16)
+    weighted_norm_kernel<__nv_bfloat16><<<grid, 256, 0, s>>>(static_cast<const __nv_bfloat16*>(X), rows, f.dim,
+                                                              f.kpad, counts, ptr, partials);
+  else
+    weighted_norm_kernel<float><<<grid, 256, 0, s>>>(static_cast<const float*>(X), rows, f.dim, f.kpad, counts,
+                                                     ptr, partials);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_partials_kernel<<<1, 256, 0, s>>>(partials, grid, out);
   return cudaGetLastError();
 }
 

@@ -339,9 +339,9 @@ __global__ void __launch_bounds__(32) nomad_replay_kernel(nomad::ReplayArgs a) {
 }
 
 // ---------------------------------------------------------------------------------
-// DSGD stratum (Code/competitor/sgd-mpi-omp.cpp:354-365): warp bi runs block
-// (bi, sched[stratum][bi]) of the innerB x innerB grid; the blocks of a stratum share
-// no row and no column.  Inside a block, ratings run in the reference's order
+// DSGD stratum (Code/competitor/sgd-mpi-omp.cpp:354-365; DSGD++ dsgdpp.cpp:403-415,
+// 444-456): warp bi runs block (bi, sched[stratum][bi]) of the innerB x col_blocks
+// grid; the blocks of a stratum share no row and no column.  Inside a block, ratings run in the reference's order
 // (sgd() walks each block from its last entry to its first; the host stores blocks
 // already reversed).  Exact form: err = (sum from index k-1 down to 0 of w*h) - v.
 // The next rating's rows are fetched ahead unless it shares the row or the column.
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(128) nomad_dsgd_kernel(nomad::DsgdArgs a, int 
   Store* __restrict__ W = static_cast<Store*>(a.f.W);
   Store* __restrict__ H = static_cast<Store*>(a.f.H);
   const int bj = a.sched[static_cast<int64_t>(stratum) * a.innerB + bi];
-  const int64_t bid = static_cast<int64_t>(bi) * a.innerB + bj;
+  const int64_t bid = static_cast<int64_t>(bi) * a.col_blocks + bj;
   const int64_t b = a.blk_ptr[bid], e = a.blk_ptr[bid + 1];
   if (b == e) return;
   const nomad::DevFactors& f = a.f;

@@ -68,9 +68,10 @@ struct ReplayArgs {
 struct DsgdArgs {
   DevFactors f;
   const int4* rates = nullptr;       // {row, col, float bits, 0} grouped by block
-  const int64_t* blk_ptr = nullptr;  // [innerB^2 + 1]
-  const int32_t* sched = nullptr;    // [innerB * innerB]: bj of row block bi in stratum i
+  const int64_t* blk_ptr = nullptr;  // [innerB * col_blocks + 1]
+  const int32_t* sched = nullptr;    // [strata * innerB]: bj of row block bi in stratum i
   int32_t innerB = 0;
+  int32_t col_blocks = 0;            // innerB (DSGD) or 2 * innerB (DSGD++)
   float step = 0.f, lambda = 0.f;
   int32_t iter = 0;
   uint32_t seed32 = 0;
@@ -160,6 +161,13 @@ cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
 cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);
 cudaError_t launch_init_hash(const DevFactors& f, uint64_t seed, cudaStream_t s);
+// Ratings per row of a CSC rating set (counts[m], zeroed first).
+cudaError_t launch_count_rows(const int2* ratings, int64_t nnz, int32_t* counts, int32_t m, cudaStream_t s);
+// *out = sum over rows r of W (rows_of_w) or H of count(r) * |x_r|^2, count from
+// counts[r] or ptr[r+1] - ptr[r]; FP64, deterministic (partials[grid] scratch).
+cudaError_t launch_weighted_norm(const DevFactors& f, bool rows_of_w, const int32_t* counts,
+                                 const int64_t* ptr, double* partials, int32_t grid, double* out,
+                                 cudaStream_t s);
 cudaError_t launch_f32_to_store(const float* src, void* dst, int64_t rows, int32_t dim,
                                 int32_t kpad, int bf16, cudaStream_t s);
 cudaError_t launch_store_to_f32(const void* src, float* dst, int64_t rows, int32_t dim,

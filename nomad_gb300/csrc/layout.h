@@ -55,8 +55,8 @@ struct AsyncLayout {
 // innerB x innerB blocks; entries of a block in reversed file order, so the device
 // walks forward through what sgd() walks backward.
 struct DsgdLayout {
-  int32_t innerB = 0, innerBm = 0, innerBn = 0;
-  std::vector<int64_t> blk_ptr;  // [innerB^2 + 1]
+  int32_t innerB = 0, col_blocks = 0, innerBm = 0, innerBn = 0;
+  std::vector<int64_t> blk_ptr;  // [innerB * col_blocks + 1]
   std::vector<int32_t> rates;    // 4 ints per entry: row, col, float bits, 0
 };
 
@@ -74,12 +74,19 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
                        int64_t priority_min, int32_t group, bool group_routes, AsyncLayout& out,
                        int threads);
 
+// innerB row blocks x col_blocks column blocks (innerB for DSGD, 2*innerB for
+// DSGD++: dsgdpp.cpp:42-52, 64-69); block (bi, bj) has id bi*col_blocks + bj.
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
-                      DsgdLayout& out);
+                      int32_t col_blocks, DsgdLayout& out);
 
 // DSGD inner-stratum schedule of iteration `iter` (1-based): bj of row block bi in
 // stratum i at [i*innerB + bi] (sgd-mpi-omp.cpp:268-365 with B = 1).
 void dsgd_schedule(int32_t innerB, int32_t iter, int32_t strategy, std::vector<int32_t>& out);
+
+// DSGD++ schedule of iteration `iter`: 2*innerB strata, phase 0 (column blocks
+// 0..innerB-1) then phase 1 (innerB..2*innerB-1); column block of row block bi in
+// stratum s at [s*innerB + bi] (dsgdpp.cpp:347-355, 393-401, 434-441 with B = 1).
+void dsgdpp_schedule(int32_t innerB, int32_t iter, int32_t strategy, std::vector<int32_t>& out);
 
 // Step size of pass `cnt` in float semantics (nomad_body.hpp:326-327).
 float step_size_f32(double lrate, double drate, int32_t cnt);

@@ -59,7 +59,7 @@ struct Options {
   std::string net_ratio = "inf";
   int verbose = 0;
   // GPU options
-  std::string mode = "async", precision = "fp32";
+  std::string mode = "async", precision = "fp32", lr_strategy = "fixed";
   int epochs = 0, workers = 0, device = 0, exact = 0, dsgd_blocks = 0;
   std::string init = "reference";
 };
@@ -99,7 +99,8 @@ const char* kUsage =
     "  --net_ratio arg (=inf)       accepted for compatibility\n"
     "  -v [ --verbose ] arg (=0)    verbose level\n"
     "GPU options:\n"
-    "  --mode arg (=async)          async | dsgd | replay\n"
+    "  --mode arg (=async)          async | dsgd | dsgdpp | replay\n"
+    "  --lr_strategy arg (=fixed)   fixed | bold (bold driver; dsgd and dsgdpp)\n"
     "  --precision arg (=fp32)      fp32 | bf16 (bf16 storage, stochastic rounding)\n"
     "  --epochs arg (=0)            train this many epochs per timeout point\n"
     "  --workers arg (=0)           async worker warps (0 = all resident)\n"
@@ -207,6 +208,7 @@ bool parse(int argc, char** argv, Options& o, bool& help) {
       else if (name == "net_ratio") o.net_ratio = v;
       else if (name == "verbose") o.verbose = std::stoi(v);
       else if (name == "mode") o.mode = v;
+      else if (name == "lr_strategy") o.lr_strategy = v;
       else if (name == "precision") o.precision = v;
       else if (name == "epochs") o.epochs = std::stoi(v);
       else if (name == "workers") o.workers = std::stoi(v);
@@ -233,7 +235,15 @@ bool parse(int argc, char** argv, Options& o, bool& help) {
   if (o.cptype != "none" && o.cpinterval <= 0) { std::cerr << "checkpoint interval is invalid.\n"; ok = false; }
   if (o.cptype != "none" && o.cppath.empty()) { std::cerr << "checkpoint path is not given.\n"; ok = false; }
   if (o.reuse != 1) { std::cerr << "only --reuse 1 is supported.\n"; ok = false; }
-  if (o.mode != "async" && o.mode != "dsgd" && o.mode != "replay") { std::cerr << "unknown --mode.\n"; ok = false; }
+  if (o.mode != "async" && o.mode != "dsgd" && o.mode != "dsgdpp" && o.mode != "replay") {
+    std::cerr << "unknown --mode.\n";
+    ok = false;
+  }
+  if (o.lr_strategy != "fixed" && o.lr_strategy != "bold") { std::cerr << "unknown --lr_strategy.\n"; ok = false; }
+  if (o.lr_strategy == "bold" && o.mode != "dsgd" && o.mode != "dsgdpp") {
+    std::cerr << "--lr_strategy bold needs --mode dsgd or dsgdpp.\n";
+    ok = false;
+  }
   if (o.precision != "fp32" && o.precision != "bf16") { std::cerr << "unknown --precision.\n"; ok = false; }
   if (o.nthreads <= 0) { std::cerr << "--nthreads must be positive.\n"; ok = false; }
   return ok;
@@ -267,7 +277,11 @@ int main(int argc, char** argv) {
   prm.drate = o.drate;
   prm.reg = o.reg;
   prm.seed = o.seed;
-  prm.mode = o.mode == "dsgd" ? NOMAD_MODE_DSGD : (o.mode == "replay" ? NOMAD_MODE_REPLAY : NOMAD_MODE_ASYNC);
+  prm.mode = o.mode == "dsgd"     ? NOMAD_MODE_DSGD
+             : o.mode == "dsgdpp" ? NOMAD_MODE_DSGDPP
+             : o.mode == "replay" ? NOMAD_MODE_REPLAY
+                                  : NOMAD_MODE_ASYNC;
+  prm.lr_strategy = o.lr_strategy == "bold" ? NOMAD_LR_BOLD_DRIVER : NOMAD_LR_FIXED;
   prm.precision = o.precision == "bf16" ? NOMAD_PREC_BF16_SR : NOMAD_PREC_FP32;
   prm.init = o.init == "hash" ? NOMAD_INIT_HASH : NOMAD_INIT_REFERENCE;
   prm.init_parts = o.nthreads;

@@ -307,18 +307,84 @@ void dsgd_schedule(int32_t innerB, int32_t iter, int32_t strategy,
   }
 }
 
+// Schedule of dsgd_mpi in dsgdpp.cpp for iteration `iter`: inner_perm / inner_offset
+// restart from the identity every iteration (dsgdpp.cpp:349-350); under WOR_STRATUM
+// phase 0 shuffles them after srand(34586 + iter) (dsgdpp.cpp:351-356, 397-400; the
+// B = 1 outer shuffles draw nothing) and phase 1 reuses them (dsgdpp.cpp:434-441).
+// bj_out[(phase*innerB + i)*innerB + bi] = phase*innerB + inner column block.
+void dsgdpp_schedule(int32_t innerB, int32_t iter, int32_t strategy,
+                     std::vector<int32_t>& bj_out) {
+  std::vector<int32_t> inner_perm(innerB), inner_offset(innerB), cur(innerB);
+  for (int32_t i = 0; i < innerB; ++i) inner_perm[i] = inner_offset[i] = cur[i] = i;
+  GlibcRand rng(34586u + static_cast<unsigned>(iter));
+  if (strategy == 2) {  // WOR_STRATUM
+    rand_shuffle(inner_perm, rng);
+    rand_shuffle(inner_offset, rng);
+  }
+  bj_out.assign(static_cast<size_t>(2) * innerB * innerB, 0);
+  for (int32_t phase = 0; phase < 2; ++phase)
+    for (int32_t i = 0; i < innerB; ++i) {
+      for (int32_t ii = 0; ii < innerB; ++ii) cur[inner_perm[ii]] = (ii + inner_offset[i]) % innerB;
+      for (int32_t bi = 0; bi < innerB; ++bi)
+        bj_out[(static_cast<size_t>(phase) * innerB + i) * innerB + bi] = phase * innerB + cur[bi];
+    }
+}
+
+// calobj_mpi (sgd-mpi-omp.cpp:122-160, the same in dsgdpp.cpp), one process: the sum
+// over training ratings of (dot(W_i, H_j) - v)^2 in double, dot summed from index
+// k-1 down to 0 (util.cpp:75-80), plus lambda * (sum_r nnz_row(r) * norm(W_r) +
+// sum_c nnz_col(c) * norm(H_c)), norm = sum of squares from index k-1 down to 0
+// (util.cpp:95-100).  Factors are read as stored.
+template <typename S>
+double objective(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                 const int32_t* cols, const double* vals, const S* W, const S* H, double reg) {
+  double loss = 0;
+  std::vector<int64_t> col_cnt(static_cast<size_t>(n), 0);
+  int64_t idx = 0;
+  for (int32_t r = 0; r < m; ++r)
+    for (int32_t t = 0; t < row_counts[r]; ++t, ++idx) {
+      const S* Wi = W + static_cast<int64_t>(dim) * r;
+      const S* Hj = H + static_cast<int64_t>(dim) * cols[idx];
+      double diff = -vals[idx];
+      double dot = 0;
+      for (int32_t kk = dim - 1; kk >= 0; --kk) dot += static_cast<double>(Wi[kk]) * static_cast<double>(Hj[kk]);
+      diff += dot;
+      loss += diff * diff;
+      col_cnt[cols[idx]]++;
+    }
+  (void)nnz;
+  auto norm = [&](const S* x) {
+    double ret = 0;
+    for (int32_t kk = dim - 1; kk >= 0; --kk) ret += static_cast<double>(x[kk]) * static_cast<double>(x[kk]);
+    return ret;
+  };
+  double regsum = 0;
+  for (int32_t r = 0; r < m; ++r) regsum += row_counts[r] * norm(W + static_cast<int64_t>(dim) * r);
+  for (int32_t c = 0; c < n; ++c) regsum += col_cnt[c] * norm(H + static_cast<int64_t>(dim) * c);
+  return loss + reg * regsum;
+}
+
+// variant 0: DSGD (sgd-mpi-omp.cpp), innerB x innerB blocks, innerB strata per pass.
+// variant 1: DSGD++ (dsgdpp.cpp), innerB x 2*innerB blocks (mpi_blocks_t,
+// dsgdpp.cpp:42-69), 2*innerB strata per pass.  lr_strategy 1 (BOLDDRIVER):
+// lr_state = {current learning rate, objective after the previous pass (< 0: not yet
+// computed)}, updated in place (sgd-mpi-omp.cpp:278-283, 384-394; dsgdpp.cpp:330-336,
+// 512-521).
 template <typename S>
 int dsgd(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
          const int32_t* cols, const double* vals, S* W, S* H, int32_t nthreads,
          int32_t first_iter, int32_t n_iters, double lrate, double decay,
-         double reg, int32_t strategy) {
+         double reg, int32_t strategy, int32_t variant = 0, int32_t lr_strategy = 0,
+         double* lr_state = nullptr) {
   if (nthreads <= 0 || dim <= 0 || first_iter < 1 || n_iters < 0) return -1;
-  const int32_t innerB = 2 * nthreads;  // sgd-mpi-omp.cpp:747
-  // mpi_blocks_t::set_parameters with B = 1 (sgd-mpi-omp.cpp:39-50)
+  if (lr_strategy == 1 && !lr_state) return -1;
+  const int32_t innerB = 2 * nthreads;  // sgd-mpi-omp.cpp:747, dsgdpp.cpp:760
+  const int32_t col_blocks = variant == 1 ? 2 * innerB : innerB;
+  // mpi_blocks_t::set_parameters with B = 1 (sgd-mpi-omp.cpp:39-50, dsgdpp.cpp:42-52)
   const int32_t Bm = m, Bn = n;
   const int32_t innerBm = Bm / innerB + ((Bm % innerB) ? 1 : 0);
-  const int32_t innerBn = Bn / innerB + ((Bn % innerB) ? 1 : 0);
-  const int32_t nblocks = innerB * innerB;
+  const int32_t innerBn = Bn / col_blocks + ((Bn % col_blocks) ? 1 : 0);
+  const int32_t nblocks = innerB * col_blocks;
   struct Rate {
     int32_t i, j;
     S v;
@@ -327,7 +393,7 @@ int dsgd(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_coun
   // the row-major entries by block id.
   std::vector<int64_t> block_ptr(nblocks + 1, 0);
   auto bid_of = [&](int32_t r, int32_t c) {
-    return (r / innerBm) * innerB + (c / innerBn);
+    return (r / innerBm) * col_blocks + (c / innerBn);
   };
   {
     int64_t idx = 0;
@@ -346,13 +412,20 @@ int dsgd(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_coun
   }
   const S lambda = static_cast<S>(reg);
   std::vector<int32_t> sched;
+  const int32_t strata = variant == 1 ? 2 * innerB : innerB;
+  if (lr_strategy == 1 && lr_state[1] < 0)
+    lr_state[1] = objective<S>(m, n, dim, nnz, row_counts, cols, vals, W, H, reg);
   for (int32_t it = first_iter; it < first_iter + n_iters; ++it) {
     // FIXED strategy (sgd-mpi-omp.cpp:308-309); lrate/decay are doubles there.
-    const S cur_lrate = static_cast<S>(1.5 * lrate / (1.0 + decay * std::pow(it, 1.5)));
-    dsgd_schedule(innerB, it, strategy, sched);
-    for (int32_t i = 0; i < innerB; ++i) {
+    const S cur_lrate = lr_strategy == 1 ? static_cast<S>(lr_state[0])
+                                         : static_cast<S>(1.5 * lrate / (1.0 + decay * std::pow(it, 1.5)));
+    if (variant == 1)
+      dsgdpp_schedule(innerB, it, strategy, sched);
+    else
+      dsgd_schedule(innerB, it, strategy, sched);
+    for (int32_t i = 0; i < strata; ++i) {
       for (int32_t bi = 0; bi < innerB; ++bi) {
-        const int32_t bid = bi * innerB + sched[static_cast<size_t>(i) * innerB + bi];
+        const int32_t bid = bi * col_blocks + sched[static_cast<size_t>(i) * innerB + bi];
         const int64_t b = block_ptr[bid], e = block_ptr[bid + 1];
         // sgd() (sgd-mpi-omp.cpp:186-210): walks the block from its last entry to its
         // first; err = dot(Wi, Hj) - v with dot summed from index k-1 down to 0.
@@ -370,6 +443,11 @@ int dsgd(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_coun
           }
         }
       }
+    }
+    if (lr_strategy == 1) {
+      const double obj = objective<S>(m, n, dim, nnz, row_counts, cols, vals, W, H, reg);
+      lr_state[0] *= obj > lr_state[1] ? decay : 1.05;
+      lr_state[1] = obj;
     }
   }
   return 0;
@@ -494,6 +572,44 @@ int oracle_dsgd_f64(int32_t m, int32_t n, int32_t dim, int64_t nnz,
                     double decay, double reg, int32_t stratum_strategy) {
   return dsgd<double>(m, n, dim, nnz, row_counts, cols, vals, W, H, nthreads,
                       first_iter, n_iters, lrate, decay, reg, stratum_strategy);
+}
+
+int oracle_dsgd2_f32(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                     const int32_t* cols, const double* vals, float* W, float* H, int32_t nthreads,
+                     int32_t first_iter, int32_t n_iters, double lrate, double decay, double reg,
+                     int32_t stratum_strategy, int32_t variant, int32_t lr_strategy, double* lr_state) {
+  return dsgd<float>(m, n, dim, nnz, row_counts, cols, vals, W, H, nthreads, first_iter, n_iters,
+                     lrate, decay, reg, stratum_strategy, variant, lr_strategy, lr_state);
+}
+int oracle_dsgd2_f64(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                     const int32_t* cols, const double* vals, double* W, double* H, int32_t nthreads,
+                     int32_t first_iter, int32_t n_iters, double lrate, double decay, double reg,
+                     int32_t stratum_strategy, int32_t variant, int32_t lr_strategy, double* lr_state) {
+  return dsgd<double>(m, n, dim, nnz, row_counts, cols, vals, W, H, nthreads, first_iter, n_iters,
+                      lrate, decay, reg, stratum_strategy, variant, lr_strategy, lr_state);
+}
+
+int oracle_objective_f32(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                         const int32_t* cols, const double* vals, const float* W, const float* H,
+                         double reg, double* out) {
+  if (dim <= 0 || !out) return -1;
+  *out = objective<float>(m, n, dim, nnz, row_counts, cols, vals, W, H, reg);
+  return 0;
+}
+int oracle_objective_f64(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                         const int32_t* cols, const double* vals, const double* W, const double* H,
+                         double reg, double* out) {
+  if (dim <= 0 || !out) return -1;
+  *out = objective<double>(m, n, dim, nnz, row_counts, cols, vals, W, H, reg);
+  return 0;
+}
+
+int oracle_dsgdpp_schedule(int32_t innerB, int32_t iter, int32_t stratum_strategy, int32_t* bj) {
+  if (innerB <= 0 || iter < 1) return -1;
+  std::vector<int32_t> s;
+  dsgdpp_schedule(innerB, iter, stratum_strategy, s);
+  std::copy(s.begin(), s.end(), bj);
+  return 0;
 }
 
 int oracle_dsgd_schedule(int32_t innerB, int32_t iter, int32_t stratum_strategy,

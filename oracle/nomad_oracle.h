@@ -16,6 +16,8 @@
  *   - file reader             Code/nomad/nb_data.cpp:19-176 (train.dat / test.dat)
  *   - DSGD                    Code/competitor/sgd-mpi-omp.cpp:186-210 (sgd), :220-424
  *                             (dsgd_mpi, single process), :35-101 (block layout)
+ *   - DSGD++, bold driver     Code/competitor/dsgdpp.cpp:300-540, :42-69 (blocks);
+ *                             sgd-mpi-omp.cpp:122-160 (calobj_mpi), :384-394
  *
  * Parity status: the reference ships no tests, fixtures or golden vectors and cannot
  * be built here (MPI/TBB/Boost/glog absent), so this restatement is pinned only by
@@ -115,6 +117,35 @@ int oracle_dsgd_f64(int32_t m, int32_t n, int32_t dim, int64_t nnz,
                     const double* vals, double* W, double* H, int32_t nthreads,
                     int32_t first_iter, int32_t n_iters, double lrate,
                     double decay, double reg, int32_t stratum_strategy);
+
+/* DSGD (variant 0) or DSGD++ (variant 1, Code/competitor/dsgdpp.cpp:300-540: innerB x
+ * 2*innerB blocks, phase 0 over the left column half then phase 1 over the right
+ * half) with the FIXED (lr_strategy 0) or BOLDDRIVER (1) learning rate.  Bold driver:
+ * lr_state = {learning rate of the next pass, objective after the previous pass or
+ * < 0 when not yet computed}, updated in place: after each pass the objective is
+ * recomputed and the rate multiplied by decay if it rose, else by 1.05. */
+int oracle_dsgd2_f32(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                     const int32_t* cols, const double* vals, float* W, float* H, int32_t nthreads,
+                     int32_t first_iter, int32_t n_iters, double lrate, double decay, double reg,
+                     int32_t stratum_strategy, int32_t variant, int32_t lr_strategy, double* lr_state);
+int oracle_dsgd2_f64(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                     const int32_t* cols, const double* vals, double* W, double* H, int32_t nthreads,
+                     int32_t first_iter, int32_t n_iters, double lrate, double decay, double reg,
+                     int32_t stratum_strategy, int32_t variant, int32_t lr_strategy, double* lr_state);
+
+/* The DSGD objective calobj_mpi (sgd-mpi-omp.cpp:122-160) of factors W, H: sum of
+ * squared errors in double plus reg * (sum_r nnz_row(r) |W_r|^2 + sum_c nnz_col(c)
+ * |H_c|^2).  Row-major rating input as oracle_dsgd_f32. */
+int oracle_objective_f32(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                         const int32_t* cols, const double* vals, const float* W, const float* H,
+                         double reg, double* out);
+int oracle_objective_f64(int32_t m, int32_t n, int32_t dim, int64_t nnz, const int32_t* row_counts,
+                         const int32_t* cols, const double* vals, const double* W, const double* H,
+                         double reg, double* out);
+
+/* DSGD++ schedule for one iteration: bj[(phase*innerB + i)*innerB + bi] is the column
+ * block (of 2*innerB) that row block bi processes in stratum i of the phase. */
+int oracle_dsgdpp_schedule(int32_t innerB, int32_t iter, int32_t stratum_strategy, int32_t* bj);
 
 /* DSGD inner-stratum schedule for one iteration: bj[i*innerB + bi] is the column
  * block that row block bi processes in inner stratum i (sgd-mpi-omp.cpp:293-365). */

@@ -58,6 +58,17 @@ def lib():
             f.restype = ctypes.c_int
             f.argtypes = [_i32, _i32, _i32, _i64, _ptr, _ptr, _ptr, _ptr, _ptr, _i32,
                           _i32, _i32, _dbl, _dbl, _dbl, _i32]
+        for name in ("oracle_dsgd2_f32", "oracle_dsgd2_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_i32, _i32, _i32, _i64, _ptr, _ptr, _ptr, _ptr, _ptr, _i32,
+                          _i32, _i32, _dbl, _dbl, _dbl, _i32, _i32, _i32, _ptr]
+        for name in ("oracle_objective_f32", "oracle_objective_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_i32, _i32, _i32, _i64, _ptr, _ptr, _ptr, _ptr, _ptr, _dbl, _ptr]
+        L.oracle_dsgdpp_schedule.restype = ctypes.c_int
+        L.oracle_dsgdpp_schedule.argtypes = [_i32, _i32, _i32, _ptr]
         L.oracle_dsgd_schedule.restype = ctypes.c_int
         L.oracle_dsgd_schedule.argtypes = [_i32, _i32, _i32, _ptr]
         L.oracle_row_major_to_csc.restype = ctypes.c_int
@@ -166,6 +177,40 @@ def dsgd(m, n, row_counts, cols, vals, W, H, nthreads, first_iter, n_iters, lrat
     f = lib().oracle_dsgd_f32 if W.dtype == np.float32 else lib().oracle_dsgd_f64
     _check(f(m, n, dim, cols.size, _p(row_counts), _p(cols), _p(vals), _p(W), _p(H),
              nthreads, first_iter, n_iters, lrate, decay, reg, stratum_strategy), "dsgd")
+
+
+def dsgd2(m, n, row_counts, cols, vals, W, H, nthreads, first_iter, n_iters, lrate, decay, reg,
+          stratum_strategy=0, variant=0, lr_strategy=0, lr_state=None):
+    """DSGD (variant 0) / DSGD++ (variant 1); lr_strategy 1 = bold driver with
+    lr_state = np.array([lrate, objective or -1]) updated in place."""
+    row_counts = np.ascontiguousarray(row_counts, np.int32)
+    cols = np.ascontiguousarray(cols, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    if lr_state is not None:
+        assert lr_state.dtype == np.float64 and lr_state.size == 2
+    dim = W.shape[1]
+    f = lib().oracle_dsgd2_f32 if W.dtype == np.float32 else lib().oracle_dsgd2_f64
+    _check(f(m, n, dim, cols.size, _p(row_counts), _p(cols), _p(vals), _p(W), _p(H),
+             nthreads, first_iter, n_iters, lrate, decay, reg, stratum_strategy, variant,
+             lr_strategy, _p(lr_state) if lr_state is not None else None), "dsgd2")
+
+
+def objective(m, n, row_counts, cols, vals, W, H, reg):
+    row_counts = np.ascontiguousarray(row_counts, np.int32)
+    cols = np.ascontiguousarray(cols, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    out = np.zeros(1, np.float64)
+    f = lib().oracle_objective_f32 if W.dtype == np.float32 else lib().oracle_objective_f64
+    _check(f(m, n, W.shape[1], cols.size, _p(row_counts), _p(cols), _p(vals), _p(W), _p(H), reg,
+             _p(out)), "objective")
+    return float(out[0])
+
+
+def dsgdpp_schedule(innerB, it, stratum_strategy=0):
+    out = np.empty(2 * innerB * innerB, np.int32)
+    _check(lib().oracle_dsgdpp_schedule(innerB, it, stratum_strategy, _p(out)),
+           "dsgdpp_schedule")
+    return out.reshape(2 * innerB, innerB)
 
 
 def dsgd_schedule(innerB, it, stratum_strategy=0):

@@ -35,7 +35,8 @@ def test_struct_sizes_match_headers(ng):
     p = ng.default_params()
     assert p.struct_size == ctypes.sizeof(ng._abi.Params)
     assert ctypes.sizeof(ng._abi.Matrix) == 48
-    assert ctypes.sizeof(ng._abi.EpochStats) == 8 * 3 + 4 * 2 + 8 * 3
+    assert ctypes.sizeof(ng._abi.EpochStats) == 8 * 3 + 4 * 2 + 8 * 5
+    assert ctypes.sizeof(ng._abi.CheckpointInfo) == 32
 
 
 def test_defaults_are_the_references(ng):

@@ -36,15 +36,18 @@ def rand_factors(m, n, dim, seed=1):
 def test_round_trip_and_layout(ng, tmp_path):
     W, H = rand_factors(7, 5, 3)
     p = str(tmp_path / "cp.ckpt")
-    ng.write_checkpoint(p, W, H, 4)
-    W2, H2, ep = ng.read_checkpoint(p)
-    assert ep == 4 and np.array_equal(W, W2) and np.array_equal(H, H2)
+    ng.write_checkpoint(p, W, H, 4, lrate=0.0125, objective=321.5)
+    W2, H2, info = ng.read_checkpoint(p, with_info=True)
+    assert info == dict(m=7, n=5, dim=3, epochs_done=4, lrate=0.0125, objective=321.5)
+    assert np.array_equal(W, W2) and np.array_equal(H, H2)
     raw = open(p, "rb").read()
     assert raw[:8] == b"NOMADCP1"
-    assert struct.unpack("<iiii", raw[8:24]) == (7, 5, 3, 4)
+    assert struct.unpack("<iiiidd", raw[8:40]) == (7, 5, 3, 4, 0.0125, 321.5)
     payload = W.tobytes() + H.tobytes()
-    assert struct.unpack("<Q", raw[24:32])[0] == fnv1a64(payload)
-    assert raw[32:] == payload
+    assert struct.unpack("<Q", raw[40:48])[0] == fnv1a64(raw[8:40] + payload)
+    assert raw[48:] == payload
+    ng.write_checkpoint(p, W, H, 1)  # no bold-driver state
+    assert ng.read_checkpoint(p, with_info=True)[2]["objective"] == -1.0
     assert not os.path.exists(p + ".tmp")
 
 
@@ -74,21 +77,21 @@ def test_format_errors(ng, tmp_path):
             if kw:
                 Wb = np.empty((kw["m"], kw["dim"]), np.float32)
                 Hb = np.empty((kw["n"], kw["dim"]), np.float32)
-                ep = ng.ctypes.c_int32()
                 ng.check(ng.lib().nomad_io_read_checkpoint(os.fsencode(str(path)), kw["m"], kw["n"],
                                                            kw["dim"], Wb.ctypes.data, Hb.ctypes.data,
-                                                           ng.ctypes.byref(ep)), "read")
+                                                           None), "read")
             else:
                 ng.read_checkpoint(str(path))
         return e.value.status
 
     assert status(b"NOMADCPX" + raw[8:]) == -7                      # magic
-    assert status(raw[:20]) == -7                                   # short header
+    assert status(raw[:44]) == -7                                   # short header
     assert status(raw[:-4]) == -7                                   # short payload
     assert status(raw + b"\0") == -7                                # trailing bytes
-    flip = bytearray(raw)
-    flip[40] ^= 1
-    assert status(bytes(flip)) == -7                                # hash
+    for pos in (30, 60):                                            # hash: header, payload
+        flip = bytearray(raw)
+        flip[pos] ^= 1
+        assert status(bytes(flip)) == -7
     neg = bytearray(raw)
     neg[8:12] = struct.pack("<i", -1)
     assert status(bytes(neg)) == -7                                 # negative size

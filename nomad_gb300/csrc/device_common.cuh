@@ -149,12 +149,21 @@ __device__ __forceinline__ uint4 pack_raw(const float (&x)[4], uint32_t, uint4*)
   return make_uint4(__float_as_uint(x[0]), __float_as_uint(x[1]), __float_as_uint(x[2]),
                     __float_as_uint(x[3]));
 }
+// Two bf16 values with stochastic rounding in one instruction: cvt.rs rounds the upper
+// element with rbits[31:16] and the lower with rbits[15:0], each as (bits(x) + r16) >> 16
+// -- the rule of f32_to_bf16_sr_bits for finite x (tests/test_sr_convert.py checks the
+// two on 2^20 random pairs); non-finite inputs saturate to the largest finite value.
+__device__ __forceinline__ uint32_t bf16x2_sr(float lo, float hi, uint32_t rbits) {
+  uint32_t d;
+  asm("cvt.rs.satfinite.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+  return d;
+}
+// Random bits per vector: one hash; value 0 takes r0[15:0], value 1 r0[31:16], value 2
+// r1[31:16] and value 3 r2[31:16] (r1, r2 odd multiples of r0).
 __device__ __forceinline__ uint2 pack_raw(const float (&x)[4], uint32_t key, uint2*) {
   const uint32_t r0 = hash32(key);
   const uint32_t r1 = r0 * 0x9E3779B1u, r2 = r0 * 0x85EBCA77u;
-  const uint32_t a = f32_to_bf16_sr_bits(x[0], r0) & 0xffffu, b = f32_to_bf16_sr_bits(x[1], r0 >> 16);
-  const uint32_t c = f32_to_bf16_sr_bits(x[2], r1 >> 16) & 0xffffu, d = f32_to_bf16_sr_bits(x[3], r2 >> 16);
-  return make_uint2(a | (b << 16), c | (d << 16));
+  return make_uint2(bf16x2_sr(x[0], x[1], r0), bf16x2_sr(x[2], x[3], __byte_perm(r1, r2, 0x7632)));
 }
 
 template <typename Store>

@@ -25,6 +25,10 @@ int host_threads(int requested = 0);
 // Run fn(t, lo, hi) on `threads` contiguous chunks of [0, count).
 void parallel_chunks(int64_t count, int threads,
                      const std::function<void(int, int64_t, int64_t)>& fn);
+// Chunks of `grain` items handed to `threads` threads on demand (for uneven items);
+// fn(thread, lo, hi) as for parallel_chunks.
+void parallel_dynamic(int64_t count, int64_t grain, int threads,
+                      const std::function<void(int, int64_t, int64_t)>& fn);
 
 // SplitMix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number generators",
 // OOPSLA 2014): a counter-based 64-bit generator, used for every seeded draw the

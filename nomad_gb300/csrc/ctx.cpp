@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -202,9 +203,25 @@ int reset_tokens(nomad_gpu_ctx* c) {
   return NOMAD_OK;
 }
 
+// Wall time of each phase of nomad_gpu_init, printed to stderr when the environment
+// variable NOMAD_TRACE_INIT is set (the setup is part of a job's end-to-end time).
+struct InitTrace {
+  bool on = std::getenv("NOMAD_TRACE_INIT") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char* phase, cudaStream_t s = nullptr) {
+    if (!on) return;
+    if (s) cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[nomad init] %-24s %8.1f ms\n", phase,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   const nomad_gpu_params& p = c->prm;
   const int threads = nomad::host_threads();
+  InitTrace trace;
   CK(cudaSetDevice(c->device));
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, c->device));
@@ -216,6 +233,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&c->ev0));
   CK(cudaEventCreate(&c->ev1));
+  trace.mark("device and stream");
 
   // ---- factors -----------------------------------------------------------------
   DevFactors& f = c->f;
@@ -255,16 +273,19 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     RC(put_factor(c, f.H, Hh.data(), f.n));
   }
 
+  trace.mark("factors (init + upload)", c->stream);
   // ---- rating sets ---------------------------------------------------------------
   nomad::Csc train, test;
   RC(nomad::build_csc(prob->train, f.m, f.n, train, threads));
   RC(nomad::build_csc(prob->test, f.m, f.n, test, threads));
+  trace.mark("CSC build");
   c->nnz_train = train.nnz();
   c->nnz_test = test.nnz();
   RC(upload_csc(c, train, &c->train, &c->train_ptr));
   RC(upload_csc(c, test, &c->test, &c->test_ptr));
   for (int32_t j = 0; j < f.n; ++j)
     c->max_column = std::max<int64_t>(c->max_column, train.col_ptr[j + 1] - train.col_ptr[j]);
+  trace.mark("CSC upload", c->stream);
 
   // ---- mode-specific layout --------------------------------------------------------
   if (p.mode == NOMAD_MODE_ASYNC) {
@@ -303,6 +324,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     nomad::AsyncLayout L;
     RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, p.exact ? 1 : c->wpb, !p.exact, L,
                                  threads));
+    trace.mark("async layout build");
     c->cta_heavy = cta_heavy && pri_min > 0;
     c->n_active = L.n_active;
     c->n_priority = L.n_priority;
@@ -359,6 +381,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   } else {
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown mode %d", p.mode);
   }
+  trace.mark("mode layout upload", c->stream);
   if (!c->err_sum) RC(dalloc(c, &c->err_sum, 1));
   c->sse_grid = c->num_sms * 8;
   RC(dalloc(c, &c->partials, c->sse_grid));
@@ -366,6 +389,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   c->cur_lr = p.lrate;
   RC(ensure_steps(c, 64));
   CK(cudaStreamSynchronize(c->stream));
+  trace.mark("scratch");
   return NOMAD_OK;
 }
 

@@ -1,6 +1,7 @@
 // host_io.cpp -- train.dat/test.dat I/O, the --output factor dump, the reference's
 // factor initialisation, and the library's host-side helpers.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -32,6 +33,27 @@ int host_threads(int requested) {
   if (requested > 0) return requested;
   unsigned hw = std::thread::hardware_concurrency();
   return hw ? static_cast<int>(hw) : 1;
+}
+
+void parallel_dynamic(int64_t count, int64_t grain, int threads,
+                      const std::function<void(int, int64_t, int64_t)>& fn) {
+  if (count <= 0) return;
+  grain = std::max<int64_t>(grain, 1);
+  const int64_t nchunks = (count + grain - 1) / grain;
+  threads = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(threads, nchunks)));
+  std::atomic<int64_t> next{0};
+  auto run = [&](int t) {
+    for (int64_t c = next.fetch_add(1); c < nchunks; c = next.fetch_add(1))
+      fn(t, c * grain, std::min(count, (c + 1) * grain));
+  };
+  if (threads == 1) {
+    run(0);
+    return;
+  }
+  std::vector<std::thread> pool;
+  pool.reserve(threads);
+  for (int t = 0; t < threads; ++t) pool.emplace_back(run, t);
+  for (auto& th : pool) th.join();
 }
 
 void parallel_chunks(int64_t count, int threads,

@@ -162,11 +162,20 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     const int64_t per = m / P + ((m % P > 0) ? 1 : 0);
     for (int32_t w = 0; w <= P; ++w) L.row_start[w] = static_cast<int32_t>(std::min<int64_t>(per * w, m));
   } else {
-    // contiguous blocks holding ~nnz/P ratings each
+    // contiguous blocks holding ~nnz/P ratings each; ratings per row from per-thread
+    // histograms (no shared counters)
+    const int nt = std::max(1, std::min<int>(threads, 64));
+    std::vector<std::vector<int32_t>> part(static_cast<size_t>(nt));
+    parallel_chunks(nnz, nt, [&](int t, int64_t lo, int64_t hi) {
+      std::vector<int32_t>& h = part[static_cast<size_t>(t)];
+      h.assign(static_cast<size_t>(m), 0);
+      for (int64_t o = lo; o < hi; ++o) ++h[csc.ratings[o].row];
+    });
     std::vector<int32_t> row_nnz(m, 0);
-    parallel_chunks(nnz, threads, [&](int, int64_t lo, int64_t hi) {
-      for (int64_t o = lo; o < hi; ++o)
-        __atomic_fetch_add(&row_nnz[csc.ratings[o].row], 1, __ATOMIC_RELAXED);
+    parallel_chunks(m, nt, [&](int, int64_t lo, int64_t hi) {
+      for (const auto& h : part)
+        if (!h.empty())
+          for (int64_t i = lo; i < hi; ++i) row_nnz[i] += h[i];
     });
     int64_t acc = 0;
     int32_t w = 1;
@@ -180,10 +189,12 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
   // visit lists: the rows of a column are ascending, so each worker's share is a run;
   // a priority column's visits are the runs of whole worker groups
   L.vl_ptr.assign(static_cast<size_t>(n) + 1, 0);
-  auto worker_of = [&](int32_t row) {
-    return static_cast<int32_t>(std::upper_bound(L.row_start.begin(), L.row_start.end(), row) -
-                                L.row_start.begin()) - 1;
-  };
+  std::vector<int32_t> row_worker(static_cast<size_t>(std::max(m, 1)));
+  parallel_chunks(P, threads, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t w = lo; w < hi; ++w)
+      for (int32_t r = L.row_start[w]; r < L.row_start[w + 1]; ++r) row_worker[r] = static_cast<int32_t>(w);
+  });
+  auto worker_of = [&](int32_t row) { return row_worker[row]; };
   auto is_priority = [&](int64_t j) {
     return priority_min > 0 && csc.col_ptr[j + 1] - csc.col_ptr[j] >= priority_min;
   };
@@ -194,8 +205,10 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     const int32_t g = w / group;
     return std::make_pair(g, L.row_start[std::min<int64_t>(static_cast<int64_t>(g + 1) * group, P)]);
   };
+  // columns are uneven (a Zipf column holds ~5% of all ratings): hand them out in small
+  // chunks on demand
   std::vector<int64_t> nseg(n, 0);
-  parallel_chunks(n, threads, [&](int, int64_t lo, int64_t hi) {
+  parallel_dynamic(n, 16, threads, [&](int, int64_t lo, int64_t hi) {
     for (int64_t j = lo; j < hi; ++j) {
       const bool pri = is_priority(j);
       int64_t c = 0;
@@ -213,7 +226,9 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
   for (int32_t j = 0; j < n; ++j) L.vl_ptr[j + 1] = L.vl_ptr[j] + nseg[j];
   L.segs.resize(static_cast<size_t>(L.vl_ptr[n]));
   std::vector<int64_t> maxseg(std::max(threads, 1), 0);
-  parallel_chunks(n, threads, [&](int t, int64_t lo, int64_t hi) {
+  parallel_dynamic(n, 16, threads, [&](int t, int64_t lo, int64_t hi) {
+    std::vector<std::pair<uint64_t, int64_t>> runs, inner;
+    std::vector<Segment> tmp;
     for (int64_t j = lo; j < hi; ++j) {
       Segment* s = L.segs.data() + L.vl_ptr[j];
       const bool pri = is_priority(j);
@@ -232,22 +247,35 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
       for (int64_t i = 0; i < k; ++i) maxseg[t] = std::max<int64_t>(maxseg[t], s[i].len);
       // the token's route: a seeded random order of its visits (pool.cpp:32-38 draws
       // a random permutation of the workers; empty visits are skipped here)
-      SplitMix64 rng(stream_key(seed, 137, static_cast<uint64_t>(j)));
-      for (int64_t i = k - 1; i > 0; --i) std::swap(s[i], s[rng.below(i + 1)]);
       if (group_routes && !pri && group > 1 && k > 1) {
         // hierarchical route: the visits to one group's workers (a thread block) stay
         // consecutive, like the reference's token that makes its round of one machine's
         // threads before it leaves for another machine (nb_main.cpp:551-565); groups and
-        // workers in a group in seeded random order
+        // workers in a group in seeded random order: visits ordered by (key of the
+        // group, key of the worker).  The visits arrive in worker order, so each group's
+        // visits are one run: order the runs by group key, then each run by worker key
+        // (keys are distinct, so they alone fix the order).
         const uint64_t kb = stream_key(seed, 149, static_cast<uint64_t>(j));
         const uint64_t kw = stream_key(seed, 151, static_cast<uint64_t>(j));
-        std::sort(s, s + k, [&](const Segment& x, const Segment& y) {
-          const uint64_t bx = SplitMix64::mix(kb ^ static_cast<uint64_t>(x.worker / group));
-          const uint64_t by = SplitMix64::mix(kb ^ static_cast<uint64_t>(y.worker / group));
-          if (bx != by) return bx < by;
-          return SplitMix64::mix(kw ^ static_cast<uint64_t>(x.worker)) <
-                 SplitMix64::mix(kw ^ static_cast<uint64_t>(y.worker));
-        });
+        runs.clear();
+        for (int64_t i = 0; i < k; ++i)
+          if (i == 0 || s[i].worker / group != s[i - 1].worker / group)
+            runs.push_back({SplitMix64::mix(kb ^ static_cast<uint64_t>(s[i].worker / group)), i});
+        std::sort(runs.begin(), runs.end());
+        tmp.assign(s, s + k);
+        int64_t o = 0;
+        for (const auto& rn : runs) {
+          const int64_t b = rn.second;
+          int64_t e = b + 1;
+          while (e < k && tmp[e].worker / group == tmp[b].worker / group) ++e;
+          inner.clear();
+          for (int64_t i = b; i < e; ++i) inner.push_back({SplitMix64::mix(kw ^ static_cast<uint64_t>(tmp[i].worker)), i});
+          std::sort(inner.begin(), inner.end());
+          for (const auto& x : inner) s[o++] = tmp[x.second];
+        }
+      } else {
+        SplitMix64 rng(stream_key(seed, 137, static_cast<uint64_t>(j)));
+        for (int64_t i = k - 1; i > 0; --i) std::swap(s[i], s[rng.below(i + 1)]);
       }
     }
   });

@@ -62,9 +62,20 @@ int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R) {
     R.cols = R.own_cols.data();
     R.v32 = R.own_vals.data();
   }
-  for (int64_t i = 0; i < A.nnz; ++i)
-    if (R.cols[i] < 0 || R.cols[i] >= n)
-      NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "column index %d out of range [0, %d)", R.cols[i], n);
+  // first out-of-range column index, checked in parallel
+  std::atomic<int64_t> bad{A.nnz};
+  const int32_t* cols = R.cols;
+  parallel_chunks(A.nnz, host_threads(), [&](int, int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i)
+      if (cols[i] < 0 || cols[i] >= n) {
+        int64_t cur = bad.load();
+        while (i < cur && !bad.compare_exchange_weak(cur, i)) {
+        }
+        break;
+      }
+  });
+  if (bad.load() < A.nnz)
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "column index %d out of range [0, %d)", cols[bad.load()], n);
   return NOMAD_OK;
 }
 
@@ -135,7 +146,7 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
   });
   // repeated cells would break the distinct-rows property a column visit relies on
   std::atomic<int64_t> dup{-1};
-  parallel_chunks(n, threads, [&](int, int64_t lo, int64_t hi) {
+  parallel_dynamic(n, 64, threads, [&](int, int64_t lo, int64_t hi) {
     for (int64_t j = lo; j < hi && dup.load(std::memory_order_relaxed) < 0; ++j)
       for (int64_t o = out.col_ptr[j] + 1; o < out.col_ptr[j + 1]; ++o)
         if (out.ratings[o].row == out.ratings[o - 1].row) {

@@ -2,6 +2,9 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "common.h"
@@ -14,12 +17,34 @@ struct Rating {
   float val;
 };
 
+// Allocator whose value construction leaves trivial elements uninitialised, so that
+// resize() of a large buffer that is filled next writes no zeros first (the first touch
+// of its pages then happens in the parallel fill).
+template <typename T>
+struct NoInitAllocator : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = NoInitAllocator<U>;
+  };
+  NoInitAllocator() = default;
+  template <typename U>
+  NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+  template <typename U>
+  void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <typename U, typename... Args>
+  void construct(U* p, Args&&... args) {
+    ::new (static_cast<void*>(p)) U(std::forward<Args>(args)...);
+  }
+};
+
 // Ratings grouped by column, rows ascending inside a column (what read_data builds
 // for one part, Code/nomad/nb_data.cpp:131-169).
 struct Csc {
   int32_t m = 0, n = 0;
   std::vector<int64_t> col_ptr;  // [n+1]
-  std::vector<Rating> ratings;   // [nnz]
+  std::vector<Rating, NoInitAllocator<Rating>> ratings;  // [nnz]
   int64_t nnz() const { return col_ptr.empty() ? 0 : col_ptr.back(); }
 };
 

@@ -13,7 +13,8 @@ whole thread blocks.  Both storage
 forms run (fp32 and bf16 with stochastic rounding); the headline value is the bf16
 form.  The device-resident number (`value`) sums CUDA-event time of the K timed epoch
 launches; `e2e` times the whole job through the C-ABI from host buffers (init with the
-H2D copy of the ratings, K epochs, an RMSE read-back per epoch, the factor read-back).
+H2D copy of the ratings, K epochs each with its online training loss and a test-RMSE
+read-back, then the final train and test RMSE and the factor read-back).
 Test RMSE is evaluated after every epoch, outside the timed launches, as the reference
 excludes testing time from training time (Code/nomad/nb_main.cpp:265-266).
 
@@ -220,8 +221,9 @@ def e2e_run(ng, train, test, K, device, args):
     nm = ng.Nomad(train, test, **kw)
     upd = 0
     for _ in range(K):
-        upd += nm.epoch(1)["updates"]
-        nm.rmse()
+        upd += nm.epoch(1)["updates"]  # the epoch's stats carry its online training loss
+        nm.rmse(train=False)           # the step's metric: test RMSE
+    nm.rmse()                          # the job's result: both RMSEs and the factors
     nm.factors()
     info = nm.info()
     nm.close()

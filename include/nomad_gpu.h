@@ -175,11 +175,13 @@ int nomad_gpu_init(nomad_gpu_ctx** out, const nomad_gpu_problem* prob,
 int nomad_gpu_epoch(nomad_gpu_ctx* ctx, int32_t n_epochs, nomad_gpu_epoch_stats* st);
 
 /* Squared-error sums and counts over the training and test sets (nb_main.cpp:617-653);
- * FP64 accumulation on the device. Any pointer may be NULL. */
+ * FP64 accumulation on the device. Any pointer may be NULL; a set whose sum and count
+ * pointers are both NULL is not evaluated (the training set is ~70x the test set). */
 int nomad_gpu_sse(nomad_gpu_ctx* ctx, double* train_sse, int64_t* train_count,
                   double* test_sse, int64_t* test_count);
 
-/* RMSE = sqrt(sse / count) for both sets (nb_main.cpp:272-275). */
+/* RMSE = sqrt(sse / count) for both sets (nb_main.cpp:272-275); a NULL output skips
+ * that set's evaluation. */
 int nomad_gpu_rmse(nomad_gpu_ctx* ctx, double* train_rmse, double* test_rmse);
 
 /* Copy the factors to host float arrays W[m*dim], H[n*dim] (either may be NULL). */

@@ -230,10 +230,12 @@ class Nomad:
                                   ctypes.byref(d)), "nomad_gpu_sse")
         return a.value, c.value, b.value, d.value
 
-    def rmse(self):
+    def rmse(self, train=True):
+        """(train RMSE, test RMSE); train=False evaluates the test set only (train is None)."""
         a, b = ctypes.c_double(), ctypes.c_double()
-        check(lib().nomad_gpu_rmse(self._ctx, ctypes.byref(a), ctypes.byref(b)), "nomad_gpu_rmse")
-        return a.value, b.value
+        check(lib().nomad_gpu_rmse(self._ctx, ctypes.byref(a) if train else None, ctypes.byref(b)),
+              "nomad_gpu_rmse")
+        return (a.value if train else None), b.value
 
     def factors(self):
         W = np.empty((self.m, self.dim), np.float32)

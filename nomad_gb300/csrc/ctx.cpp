@@ -700,14 +700,16 @@ int nomad_gpu_sse(nomad_gpu_ctx* c, double* train_sse, int64_t* train_count, dou
   a.f = c->f;
   a.partials = c->partials;
   a.grid = c->sse_grid;
+  // a set whose two outputs are both NULL is not evaluated
+  const bool want_train = train_sse || train_count, want_test = test_sse || test_count;
   a.ratings = c->train;
   a.col_ptr = c->train_ptr;
-  a.nnz = c->nnz_train;
+  a.nnz = want_train ? c->nnz_train : 0;
   a.out = c->sse_out;
   CK(nomad::launch_sse(a, c->stream));
   a.ratings = c->test;
   a.col_ptr = c->test_ptr;
-  a.nnz = c->nnz_test;
+  a.nnz = want_test ? c->nnz_test : 0;
   a.out = c->sse_out + 1;
   CK(nomad::launch_sse(a, c->stream));
   double h[2];
@@ -724,7 +726,8 @@ int nomad_gpu_sse(nomad_gpu_ctx* c, double* train_sse, int64_t* train_count, dou
 int nomad_gpu_rmse(nomad_gpu_ctx* c, double* train_rmse, double* test_rmse) {
   double s0 = 0, s1 = 0;
   int64_t c0 = 0, c1 = 0;
-  int rc = nomad_gpu_sse(c, &s0, &c0, &s1, &c1);
+  int rc = nomad_gpu_sse(c, train_rmse ? &s0 : nullptr, train_rmse ? &c0 : nullptr, test_rmse ? &s1 : nullptr,
+                         test_rmse ? &c1 : nullptr);
   if (rc) return rc;
   if (train_rmse) *train_rmse = c0 ? std::sqrt(s0 / c0) : NAN;
   if (test_rmse) *test_rmse = c1 ? std::sqrt(s1 / c1) : NAN;

@@ -66,6 +66,8 @@ def parse():
                     help="netflix: the headline 480,189 x 17,770 workload; batched: the "
                          "4,096-problem batch (a separate line, not the headline)")
     ap.add_argument("--count", type=int, default=4096, help="problems in the batched workload")
+    ap.add_argument("--no-ttt", action="store_true",
+                    help="skip the time-to-target runs (fresh contexts trained to the FP64 target)")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink rows, columns and ratings by this factor (profiling captures "
                          "of a smaller case of the same shape; not a headline number)")
@@ -195,22 +197,32 @@ def run_form(ng, train, test, precision, W, K, device, args, clocks=None):
             "host_updates_per_s": upd / max(sum(x["host_s"] for x in timed), 1e-12)}
 
 
-def time_to_target(res, curve):
-    """Training seconds (device) until test RMSE <= 1.005 x the FP64 oracle's RMSE at the
-    last epoch run, and the largest per-epoch gap to the oracle at equal epochs."""
+def time_to_target(ng, train, test, form, curve, device, args, max_epochs=40):
+    """Device seconds of training until the test RMSE is within 0.5% of the FP64 oracle's
+    RMSE after all of its epochs (the committed 20-epoch trajectory of the same workload,
+    init and hyper-parameters): a fresh context trains epoch by epoch, reading the test
+    RMSE after each, until it reaches 1.005 x that RMSE or `max_epochs` pass.  Also the
+    gap to the oracle at equal epochs (largest, and at the oracle's last epoch)."""
     if not curve:
         return None
     ref = curve["test_rmse"]
-    E = min(len(res["epochs"]), len(ref))
-    target = ref[E - 1] * 1.005
-    t, hit = 0.0, None
-    for e in range(E):
-        t += res["epochs"][e]["device_ms"] / 1e3
-        if hit is None and res["epochs"][e]["test_rmse"] <= target:
-            hit = t
-    gaps = [abs(res["epochs"][e]["test_rmse"] - ref[e]) / ref[e] for e in range(E)]
-    return {"seconds": hit, "target_rmse": target, "oracle_epochs": E,
-            "final_gap": gaps[-1], "max_gap": max(gaps)}
+    target = ref[-1] * 1.005
+    kw = dict(HP, precision=form, mode="async", device=device, init_parts=16,
+              workers=args.workers, warps_per_block=args.wpb, blocks_per_sm=args.bps)
+    t, hit, hit_epochs, gaps = 0.0, None, None, []
+    with ng.Nomad(train, test, **kw) as nm:
+        for e in range(max_epochs):
+            t += nm.epoch(1)["device_ms"] / 1e3
+            te = nm.rmse(train=False)[1]
+            if e < len(ref):
+                gaps.append(abs(te - ref[e]) / ref[e])
+            if te <= target:
+                hit, hit_epochs = t, e + 1
+                if e + 1 >= len(ref):
+                    break
+    return {"seconds": hit, "epochs": hit_epochs, "target_rmse": target,
+            "oracle_epochs": len(ref), "gap_at_oracle_epochs": gaps[len(ref) - 1] if len(gaps) >= len(ref) else None,
+            "max_gap": max(gaps) if gaps else None}
 
 
 def e2e_run(ng, train, test, K, device, args):
@@ -346,6 +358,7 @@ def main_ours(args, dist):
     except (OSError, KeyError, ValueError):
         pass
     curve = target_curve()
+    ttt = None if args.no_ttt else {f: time_to_target(ng, train, test, f, curve, device, args) for f in forms}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
         "steps": K, "warmup": W, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
@@ -358,8 +371,7 @@ def main_ours(args, dist):
                  "final_test_rmse": res["fp32"]["epochs"][-1]["test_rmse"]},
         "bf16_over_fp32": b["updates_per_s"] / res["fp32"]["updates_per_s"],
         "final_test_rmse": b["epochs"][-1]["test_rmse"],
-        "time_to_target": {"bf16": time_to_target(b, curve),
-                           "fp32": time_to_target(res["fp32"], curve)},
+        "time_to_target": ttt,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"of {peak_kind}",

@@ -35,6 +35,13 @@ def test_bad_value_and_unknown_option(ng):
     assert r.returncode == 1 and "checkpoint type is inalid." in r.stderr
 
 
+def test_mode_options_are_validated(ng):
+    r = run("--path", "x", "--mode", "async", "--lr_strategy", "bold")
+    assert r.returncode == 1 and "--lr_strategy bold needs --mode dsgd or dsgdpp." in r.stderr
+    assert run("--path", "x", "--mode", "sgd").returncode == 1
+    assert "dsgdpp" in run("--help").stderr
+
+
 def test_checkpoint_options_are_validated(ng):
     """nomad_option.cpp:100-111: a checkpoint type needs a positive interval and a path."""
     r = run("--path", "x", "--cptype", "sync")
@@ -148,3 +155,17 @@ def test_checkpoint_and_recover(ng, gpu_ok, tmp_path):
     assert open(tmp_path / "resumed0").read() == open(tmp_path / "straight0").read()
     r3 = run(*common, "--epochs", "1", "--recover", "5", "--cppath", str(cp), "--jobid", "7")
     assert r3.returncode == 1 and "error in restoring checkpoint" in r3.stderr
+
+
+@pytest.mark.gpu
+def test_dsgdpp_and_bold_driver_modes(ng, gpu_ok, tmp_path):
+    """--mode dsgdpp and --lr_strategy bold (DSGD and DSGD++ only) run end to end."""
+    tr, _ = _write_dataset(ng, str(tmp_path))
+    for mode, lr in (("dsgdpp", "fixed"), ("dsgdpp", "bold"), ("dsgd", "bold")):
+        r = run("--path", str(tmp_path), "--dim", "8", "--epochs", "3", "--pause", "0",
+                "--mode", mode, "--lr_strategy", lr, "--reg", "0.05", "--lrate", "0.01")
+        assert r.returncode == 0, (mode, lr, r.stderr)
+        st = _stats(r.stdout)
+        assert int(st[0][4]) == 3 * tr.nnz
+    r = run("--path", str(tmp_path), "--mode", "async", "--lr_strategy", "bold")
+    assert r.returncode == 1 and "--lr_strategy bold needs --mode dsgd or dsgdpp." in r.stderr

@@ -23,6 +23,7 @@ oracle's asynchronous float mode, every host core) on the same workload: the ref
 itself needs MPI, TBB, Boost and glog, none of which exist on these machines.
 """
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import statistics
@@ -399,7 +400,8 @@ def main_batched(args, dist):
     device = dist.local
     K, W = args.steps, args.warmup
     t = time.perf_counter()
-    probs = [ng.synth_batch_problem(i) for i in range(args.count)]
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:  # one generator thread each
+        probs = list(ex.map(lambda i: ng.synth_batch_problem(i, threads=1), range(args.count)))
     nnz = sum(p[0].nnz for p in probs)
     log(f"[bench] {args.count} problems ({nnz} train ratings) generated in {time.perf_counter() - t:.1f} s")
     kw = dict(lrate=0.002, drate=0.1, reg=0.05, device=device)

@@ -128,12 +128,14 @@ def synth(workload_or_spec, **overrides):
     return RatingMatrix._from_io(tr), RatingMatrix._from_io(te)
 
 
-def synth_batch_problem(index, seed=12345):
+def synth_batch_problem(index, seed=12345, threads=0):
     """Problem `index` of the batched workload (4,096 problems of uneven shape and rank):
-    (train, test, dim)."""
+    (train, test, dim).  `threads` generator threads (0: every core); the data does not
+    depend on it."""
     spec, dim = _abi.SynthSpec(), ctypes.c_int32()
     check(lib().nomad_synth_batch_problem(int(seed), int(index), ctypes.byref(spec),
                                           ctypes.byref(dim)), "nomad_synth_batch_problem")
+    spec.threads = int(threads)
     train, test = synth(spec)
     return train, test, dim.value
 

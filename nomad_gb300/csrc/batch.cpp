@@ -8,11 +8,13 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "common.h"
 #include "launch.h"
 #include "layout.h"
+#include "trace.h"
 
 struct nomad_gpu_batch {
   nomad_gpu_params prm{};
@@ -117,6 +119,7 @@ int ensure_graph(nomad_gpu_batch* b) {
 int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t count) {
   const nomad_gpu_params& p = b->prm;
   const int threads = nomad::host_threads();
+  nomad::InitTrace trace;
   CK(cudaSetDevice(b->device));
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, b->device));
@@ -131,21 +134,37 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   b->esz = bf16 ? 2 : 4;
 
   // ---- per-problem layout, concatenated ------------------------------------------------
+  // Each problem's CSC is built on one thread, problems handed out on demand; the
+  // concatenated arrays are then sized by prefix sums and filled in parallel.
   b->probs.resize(count);
-  std::vector<nomad::Rating> tr_all, te_all;  // {int32 row, float value}: the device's int2
-  std::vector<int64_t> cp_all, tcp_all;
-  std::vector<int64_t> nnz(count);
-  std::vector<nomad::Csc> csc_keep;  // large-problem candidates need their CSC below
-  csc_keep.resize(count);
-  int64_t w_off = 0, h_off = 0;
-  int64_t max_rows = 0;
   for (int32_t i = 0; i < count; ++i) {
     const nomad_gpu_batch_problem& q = P[i];
     if (q.m <= 0 || q.n <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "problem %d: m and n must be positive", i);
     if (q.dim <= 0 || q.dim > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "problem %d: dim %d outside [1, 128]", i, q.dim);
-    nomad::Csc tr, te;
-    RC(nomad::build_csc(q.train, q.m, q.n, tr, threads));
-    RC(nomad::build_csc(q.test, q.m, q.n, te, threads));
+  }
+  std::vector<nomad::Csc> csc_tr(count), csc_te(count);
+  std::vector<int> status(count, NOMAD_OK);
+  std::vector<std::string> errors(count);
+  nomad::parallel_dynamic(count, 4, threads, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      const nomad_gpu_batch_problem& q = P[i];
+      int rc = nomad::build_csc(q.train, q.m, q.n, csc_tr[i], 1);
+      if (!rc) rc = nomad::build_csc(q.test, q.m, q.n, csc_te[i], 1);
+      if (rc) {
+        status[i] = rc;
+        errors[i] = nomad::last_error();
+      }
+    }
+  });
+  for (int32_t i = 0; i < count; ++i)
+    if (status[i]) NOMAD_FAIL(status[i], "problem %d: %s", i, errors[i].c_str());
+  trace.mark("CSC builds");
+  std::vector<int64_t> nnz(count);
+  int64_t w_off = 0, h_off = 0, tr_len = 0, te_len = 0, cp_len = 0, tcp_len = 0;
+  int64_t max_rows = 0;
+  std::vector<int64_t> tr_at(count), te_at(count);
+  for (int32_t i = 0; i < count; ++i) {
+    const nomad_gpu_batch_problem& q = P[i];
     nomad::BatchProblem& pb = b->probs[i];
     std::memset(&pb, 0, sizeof(pb));
     pb.m = q.m;
@@ -160,19 +179,36 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     w_off += static_cast<int64_t>(q.m) * pb.kpad;
     h_off += static_cast<int64_t>(q.n) * pb.kpad;
     max_rows = std::max<int64_t>(max_rows, std::max(q.m, q.n));
-    pb.col_off = static_cast<int64_t>(cp_all.size());
-    pb.test_col_off = static_cast<int64_t>(tcp_all.size());
-    const int64_t tb = static_cast<int64_t>(tr_all.size()), eb = static_cast<int64_t>(te_all.size());
-    for (int64_t c : tr.col_ptr) cp_all.push_back(tb + c);
-    for (int64_t c : te.col_ptr) tcp_all.push_back(eb + c);
-    tr_all.insert(tr_all.end(), tr.ratings.begin(), tr.ratings.end());
-    te_all.insert(te_all.end(), te.ratings.begin(), te.ratings.end());
-    nnz[i] = tr.nnz();
-    int32_t act = 0;
-    for (int32_t j = 0; j < q.n; ++j) act += tr.col_ptr[j + 1] > tr.col_ptr[j] ? 1 : 0;
-    pb.n_active = act;
-    csc_keep[i] = std::move(tr);
+    pb.col_off = cp_len;
+    pb.test_col_off = tcp_len;
+    cp_len += q.n + 1;
+    tcp_len += q.n + 1;
+    tr_at[i] = tr_len;
+    te_at[i] = te_len;
+    nnz[i] = csc_tr[i].nnz();
+    tr_len += nnz[i];
+    te_len += csc_te[i].nnz();
   }
+  std::vector<nomad::Rating, nomad::NoInitAllocator<nomad::Rating>> tr_all(tr_len), te_all(te_len);  // device int2
+  std::vector<int64_t> cp_all(cp_len), tcp_all(tcp_len);
+  nomad::parallel_dynamic(count, 4, threads, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      nomad::BatchProblem& pb = b->probs[i];
+      const nomad::Csc& tr = csc_tr[i];
+      const nomad::Csc& te = csc_te[i];
+      for (int32_t j = 0; j <= pb.n; ++j) {
+        cp_all[pb.col_off + j] = tr_at[i] + tr.col_ptr[j];
+        tcp_all[pb.test_col_off + j] = te_at[i] + te.col_ptr[j];
+      }
+      std::copy(tr.ratings.begin(), tr.ratings.end(), tr_all.begin() + tr_at[i]);
+      std::copy(te.ratings.begin(), te.ratings.end(), te_all.begin() + te_at[i]);
+      int32_t act = 0;
+      for (int32_t j = 0; j < pb.n; ++j) act += tr.col_ptr[j + 1] > tr.col_ptr[j] ? 1 : 0;
+      pb.n_active = act;
+    }
+  });
+  csc_te.clear();
+  trace.mark("concatenation");
   // work queue: the largest problems first, so the longest epochs start first
   std::vector<int32_t> order(count);
   std::iota(order.begin(), order.end(), 0);
@@ -197,38 +233,47 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     while (n_big < count && nnz[order[n_big]] >= big_min && P[order[n_big]].n < nomad::kBatchRing &&
            P[order[n_big]].n < 65536)
       ++n_big;
+    // slices: R + 1 row starts and n (R + 1) visit offsets per large problem
+    int64_t seg_len = 0;
     for (int32_t t = 0; t < n_big; ++t) {
-      const int32_t i = order[t];
-      const nomad::Csc& c = csc_keep[i];
-      nomad::BatchProblem& pb = b->probs[i];
-      std::vector<int64_t> row_nnz(pb.m, 0);
-      for (const auto& r : c.ratings) ++row_nnz[r.row];
-      pb.rs_off = static_cast<int32_t>(rs_all.size());
-      const int64_t nz = c.nnz();
-      int64_t acc = 0;
-      int32_t r = 1;
-      rs_all.push_back(0);
-      for (int32_t row = 0; row < pb.m && r < R; ++row) {
-        acc += row_nnz[row];
-        while (r < R && acc >= (nz * r + R - 1) / R) {
-          rs_all.push_back(row + 1);
-          ++r;
-        }
-      }
-      for (; r <= R; ++r) rs_all.push_back(pb.m);
-      const int32_t* rs = rs_all.data() + pb.rs_off;
-      pb.seg_off = static_cast<int64_t>(seg_all.size());
-      const int64_t cbase = cp_all[pb.col_off];  // absolute offset of the problem's ratings
-      for (int32_t j = 0; j < pb.n; ++j) {
-        int64_t o = c.col_ptr[j];
-        for (int32_t w = 0; w <= R; ++w) {
-          while (o < c.col_ptr[j + 1] && c.ratings[o].row < rs[w]) ++o;
-          seg_all.push_back(cbase + o);
-        }
-      }
+      nomad::BatchProblem& pb = b->probs[order[t]];
+      pb.rs_off = t * (R + 1);
+      pb.seg_off = seg_len;
+      seg_len += static_cast<int64_t>(pb.n) * (R + 1);
     }
+    rs_all.assign(static_cast<size_t>(n_big) * (R + 1), 0);
+    seg_all.assign(static_cast<size_t>(seg_len), 0);
+    nomad::parallel_dynamic(n_big, 1, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t t = lo; t < hi; ++t) {
+        const int32_t i = order[t];
+        const nomad::Csc& c = csc_tr[i];
+        const nomad::BatchProblem& pb = b->probs[i];
+        std::vector<int64_t> row_nnz(pb.m, 0);
+        for (const auto& r : c.ratings) ++row_nnz[r.row];
+        int32_t* rs = rs_all.data() + pb.rs_off;
+        const int64_t nz = c.nnz();
+        int64_t acc = 0;
+        int32_t r = 1;
+        rs[0] = 0;
+        for (int32_t row = 0; row < pb.m && r < R; ++row) {
+          acc += row_nnz[row];
+          while (r < R && acc >= (nz * r + R - 1) / R) rs[r++] = row + 1;
+        }
+        for (; r <= R; ++r) rs[r] = pb.m;
+        const int64_t cbase = cp_all[pb.col_off];  // absolute offset of the problem's ratings
+        int64_t* sg = seg_all.data() + pb.seg_off;
+        for (int32_t j = 0; j < pb.n; ++j) {
+          int64_t o = c.col_ptr[j];
+          for (int32_t w = 0; w <= R; ++w) {
+            while (o < c.col_ptr[j + 1] && c.ratings[o].row < rs[w]) ++o;
+            *sg++ = cbase + o;
+          }
+        }
+      }
+    });
   }
-  csc_keep.clear();
+  csc_tr.clear();
+  trace.mark("large-problem layout");
 
   nomad::BatchArgs& a = b->a;
   a.count = count;
@@ -284,30 +329,60 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     CK(cudaMemsetAsync(a.ring_ctr, 0, static_cast<size_t>(b->grid) * R * sizeof(unsigned), b->stream));
   }
 
-  // ---- factors: given, or the reference init of each problem, through one staging buffer
+  trace.mark("uploads", b->stream);
+  // ---- factors: given, or the reference init of each problem.  Problems go in groups
+  // of at most kStage floats: the group's dense fp32 rows are generated in parallel on the
+  // host, copied once, and converted to the padded storage per problem on the device.
+  constexpr int64_t kStage = int64_t(1) << 26;  // 256 MB of fp32
   float* stage = nullptr;
-  RC(dalloc(b, &stage, static_cast<size_t>(max_rows) * 128));
-  std::vector<float> hw;
-  for (int32_t i = 0; i < count; ++i) {
-    const nomad_gpu_batch_problem& q = P[i];
-    const nomad::BatchProblem& pb = b->probs[i];
-    for (int side = 0; side < 2; ++side) {
-      const int64_t rows = side ? q.n : q.m;
-      const float* src = side ? q.H0 : q.W0;
-      if (!src) {
-        hw.assign(static_cast<size_t>(rows) * q.dim, 0.f);
-        RC(nomad_reference_init(side ? 0 : q.m, side ? q.n : 0, q.dim, p.seed, std::max(p.init_parts, 1),
-                                side ? nullptr : hw.data(), side ? hw.data() : nullptr));
-        src = hw.data();
-      }
-      CK(cudaMemcpyAsync(stage, src, static_cast<size_t>(rows) * q.dim * sizeof(float), cudaMemcpyHostToDevice,
-                         b->stream));
-      char* dst = (side ? H : W) + (side ? pb.h_off : pb.w_off) * b->esz;
-      CK(nomad::launch_f32_to_store(stage, dst, rows, q.dim, pb.kpad, bf16, b->stream));
-      CK(cudaStreamSynchronize(b->stream));  // the staging buffer is reused
+  int64_t stage_len = 0;
+  for (int32_t i = 0; i < count; ++i)
+    stage_len = std::max<int64_t>(stage_len, static_cast<int64_t>(P[i].m + P[i].n) * P[i].dim);
+  stage_len = std::max(stage_len, std::min<int64_t>(kStage, (w_off + h_off)));
+  RC(dalloc(b, &stage, static_cast<size_t>(stage_len)));
+  std::vector<float, nomad::NoInitAllocator<float>> host(static_cast<size_t>(stage_len));
+  for (int32_t g0 = 0; g0 < count;) {
+    // the group [g0, g1): consecutive problems whose rows fit the staging buffer
+    std::vector<int64_t> at;
+    int64_t used = 0;
+    int32_t g1 = g0;
+    while (g1 < count) {
+      const int64_t need = static_cast<int64_t>(P[g1].m + P[g1].n) * P[g1].dim;
+      if (g1 > g0 && used + need > stage_len) break;
+      at.push_back(used);
+      used += need;
+      ++g1;
     }
+    nomad::parallel_dynamic(g1 - g0, 1, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t t = lo; t < hi; ++t) {
+        const nomad_gpu_batch_problem& q = P[g0 + t];
+        float* Wh = host.data() + at[t];
+        float* Hh = Wh + static_cast<int64_t>(q.m) * q.dim;
+        if (q.W0)
+          std::copy(q.W0, q.W0 + static_cast<int64_t>(q.m) * q.dim, Wh);
+        else
+          nomad_reference_init(q.m, 0, q.dim, p.seed, std::max(p.init_parts, 1), Wh, nullptr);
+        if (q.H0)
+          std::copy(q.H0, q.H0 + static_cast<int64_t>(q.n) * q.dim, Hh);
+        else
+          nomad_reference_init(0, q.n, q.dim, p.seed, std::max(p.init_parts, 1), nullptr, Hh);
+      }
+    });
+    CK(cudaMemcpyAsync(stage, host.data(), static_cast<size_t>(used) * sizeof(float), cudaMemcpyHostToDevice,
+                       b->stream));
+    for (int32_t i = g0; i < g1; ++i) {
+      const nomad_gpu_batch_problem& q = P[i];
+      const nomad::BatchProblem& pb = b->probs[i];
+      const float* src = stage + at[i - g0];
+      CK(nomad::launch_f32_to_store(src, W + pb.w_off * b->esz, q.m, q.dim, pb.kpad, bf16, b->stream));
+      CK(nomad::launch_f32_to_store(src + static_cast<int64_t>(q.m) * q.dim, H + pb.h_off * b->esz, q.n, q.dim,
+                                    pb.kpad, bf16, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));  // the host and device staging buffers are reused
+    g0 = g1;
   }
 
+  trace.mark("factors");
   b->sse_grid = std::max(1, std::min((count + 3) / 4, 8 * b->num_sms));
   RC(ensure_steps(b, 64));
   CK(cudaStreamSynchronize(b->stream));

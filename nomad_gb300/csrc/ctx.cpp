@@ -12,6 +12,7 @@
 
 #include "common.h"
 #include "launch.h"
+#include "trace.h"
 #include "layout.h"
 
 using nomad::DevFactors;
@@ -203,25 +204,10 @@ int reset_tokens(nomad_gpu_ctx* c) {
   return NOMAD_OK;
 }
 
-// Wall time of each phase of nomad_gpu_init, printed to stderr when the environment
-// variable NOMAD_TRACE_INIT is set (the setup is part of a job's end-to-end time).
-struct InitTrace {
-  bool on = std::getenv("NOMAD_TRACE_INIT") != nullptr;
-  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
-  void mark(const char* phase, cudaStream_t s = nullptr) {
-    if (!on) return;
-    if (s) cudaStreamSynchronize(s);
-    const auto now = std::chrono::steady_clock::now();
-    std::fprintf(stderr, "[nomad init] %-24s %8.1f ms\n", phase,
-                 std::chrono::duration<double, std::milli>(now - t).count());
-    t = now;
-  }
-};
-
 int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   const nomad_gpu_params& p = c->prm;
   const int threads = nomad::host_threads();
-  InitTrace trace;
+  nomad::InitTrace trace;
   CK(cudaSetDevice(c->device));
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, c->device));

@@ -26,7 +26,7 @@ struct RowMajor {
   float val(int64_t i) const { return v64 ? static_cast<float>(v64[i]) : v32[i]; }
 };
 
-int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R) {
+int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R, int threads) {
   if (A.nnz < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "negative nnz");
   if (A.nnz > 0 && (!A.cols || (!A.vals_f64 && !A.vals_f32)))
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "rating set has nnz > 0 but null arrays");
@@ -65,7 +65,7 @@ int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R) {
   // first out-of-range column index, checked in parallel
   std::atomic<int64_t> bad{A.nnz};
   const int32_t* cols = R.cols;
-  parallel_chunks(A.nnz, host_threads(), [&](int, int64_t lo, int64_t hi) {
+  parallel_chunks(A.nnz, threads, [&](int, int64_t lo, int64_t hi) {
     for (int64_t i = lo; i < hi; ++i)
       if (cols[i] < 0 || cols[i] >= n) {
         int64_t cur = bad.load();
@@ -106,7 +106,7 @@ float step_size_f32(double lrate, double drate, int32_t cnt) {
 
 int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int threads) {
   RowMajor R;
-  int rc = to_row_major(A, m, n, R);
+  int rc = to_row_major(A, m, n, R, threads);
   if (rc) return rc;
   const int64_t nnz = A.nnz;
   out.m = m;
@@ -338,7 +338,7 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,
                       int32_t col_blocks, DsgdLayout& D) {
   RowMajor R;
-  int rc = to_row_major(A, m, n, R);
+  int rc = to_row_major(A, m, n, R, host_threads());
   if (rc) return rc;
   if (innerB <= 0 || col_blocks <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "DSGD needs innerB > 0");
   D.innerB = innerB;

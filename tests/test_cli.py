@@ -169,3 +169,25 @@ def test_dsgdpp_and_bold_driver_modes(ng, gpu_ok, tmp_path):
         assert int(st[0][4]) == 3 * tr.nnz
     r = run("--path", str(tmp_path), "--mode", "async", "--lr_strategy", "bold")
     assert r.returncode == 1 and "--lr_strategy bold needs --mode dsgd or dsgdpp." in r.stderr
+
+
+@pytest.mark.gpu
+def test_recover_keeps_the_bold_driver_rate(ng, gpu_ok, tmp_path):
+    """A DSGD++ bold-driver run resumed from its checkpoint continues with the saved rate
+    and objective: its factor dump equals the uninterrupted run's."""
+    data, cp = tmp_path / "data", tmp_path / "cp"
+    data.mkdir()
+    cp.mkdir()
+    _write_dataset(ng, str(data))
+    common = ("--path", str(data), "--dim", "8", "--lrate", "0.05", "--drate", "0.5", "--reg", "0.05",
+              "--pause", "0", "--mode", "dsgdpp", "--lr_strategy", "bold", "--tm_interval", "1e9")
+    r = run(*common, "--epochs", "2", "--cptype", "sync", "--cpinterval", "1e-9", "--cppath", str(cp))
+    assert r.returncode == 0, r.stderr
+    info = ng.read_checkpoint(str(cp / "cp-t1-e1.ckpt"), with_info=True)[2]
+    assert info["epochs_done"] == 2 and info["lrate"] > 0 and info["objective"] > 0
+    r1 = run(*common, "--epochs", "1", "--recover", "1", "--cppath", str(cp),
+             "--output", str(tmp_path / "resumed"))
+    assert r1.returncode == 0, r1.stderr
+    r2 = run(*common, "--epochs", "3", "--output", str(tmp_path / "straight"))
+    assert r2.returncode == 0, r2.stderr
+    assert open(tmp_path / "resumed0").read() == open(tmp_path / "straight0").read()

@@ -308,10 +308,11 @@ def test_dsgdpp_fast_rmse(ng, O, gpu_ok):
 
 
 @pytest.mark.gpu
-def test_bold_driver_resume_is_bit_exact(ng, gpu_ok, tmp_path):
+@pytest.mark.parametrize("mode,precision", [("dsgdpp", "fp32"), ("dsgdpp", "bf16"), ("dsgd", "bf16")])
+def test_bold_driver_resume_is_bit_exact(ng, gpu_ok, tmp_path, mode, precision):
     train, test = _problem(ng, seed=11)
-    kw = dict(dim=16, lrate=0.02, drate=0.5, reg=REG, mode="dsgdpp", lr_strategy="bold",
-              dsgd_inner_blocks=8)
+    kw = dict(dim=16, lrate=0.02, drate=0.5, reg=REG, mode=mode, lr_strategy="bold",
+              dsgd_inner_blocks=8, precision=precision)
     with ng.Nomad(train, test, **kw) as a:
         a.epoch(4)
         Wa, Ha = a.factors()

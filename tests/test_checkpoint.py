@@ -179,3 +179,25 @@ def test_set_epochs_done_sets_the_step(ng, gpu_ok):
     with ng.Nomad(train, test, W0=W2, H0=H2, **kw) as c:
         c.epoch(1)
         assert not np.array_equal(c.factors()[0], W3)
+
+
+@pytest.mark.gpu
+def test_load_rejects_mismatched_checkpoints(ng, gpu_ok, tmp_path):
+    """A checkpoint of another shape, or one without bold-driver state for a bold-driver
+    context, is an invalid argument and leaves the context usable."""
+    train, test = _problem(ng, seed=6)
+    p = str(tmp_path / "cp.ckpt")
+    with ng.Nomad(train, test, dim=8, lrate=LR, drate=DR, reg=REG, mode="replay") as a:
+        a.epoch(1)
+        a.save_checkpoint(p)
+    with ng.Nomad(train, test, dim=16, lrate=LR, drate=DR, reg=REG, mode="replay") as b:
+        with pytest.raises(ng.NomadError) as e:
+            b.load_checkpoint(p)
+        assert e.value.status == -1
+        assert b.epoch(1)["epochs_done"] == 1
+    with ng.Nomad(train, test, dim=8, lrate=LR, drate=0.5, reg=REG, mode="dsgd",
+                  lr_strategy="bold", dsgd_inner_blocks=4) as c:
+        with pytest.raises(ng.NomadError) as e:
+            c.load_checkpoint(p)
+        assert e.value.status == -1 and "bold-driver" in str(e.value)
+        assert c.epoch(1)["epochs_done"] == 1

@@ -276,23 +276,33 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   // ---- mode-specific layout --------------------------------------------------------
   if (p.mode == NOMAD_MODE_ASYNC) {
     // exact kernel: up to 8 worker warps per block; pipelined kernel: up to 14 compute
-    // warps (workers) plus the pop and push warps
+    // warps (workers) plus the pop and push warps, fewer where the kernel was compiled
+    // for smaller blocks (10 for fp32 rows, 12 for bf16: the occupancy query says so)
     if (p.exact)
       c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 8) : 8;
     else
       c->wpb = p.warps_per_block > 0 ? std::min(p.warps_per_block, 14) : 14;
     const int nv = f.nvec <= 32 ? 1 : (f.nvec <= 64 ? 2 : 4);
     // pipelined kernel: long columns visit whole thread blocks (unless priority is off)
-    const int cta_heavy = !p.exact && p.priority_permille >= 0 ? 1 : 0;
+    int cta_heavy = !p.exact && p.priority_permille >= 0 ? 1 : 0;
     int bps = 0;
     if (p.exact) {
       CK(nomad::async_occupancy(f.bf16, nv, 1, c->wpb, f.kpad, &bps));
     } else {
-      // fewer compute warps per block when long rows do not fit the shared memory
+      // fewer compute warps per block when long rows do not fit the shared memory, and
+      // no block visits when their staged rows do not fit even beside one warp
+      const int wpb0 = c->wpb;
       while (true) {
         CK(nomad::async2_occupancy(f.bf16, nv, c->wpb, f.kpad, cta_heavy, &bps));
-        if (bps > 0 || c->wpb == 1) break;
-        --c->wpb;
+        if (bps > 0) break;
+        if (c->wpb > 1) {
+          --c->wpb;
+        } else if (cta_heavy) {
+          cta_heavy = 0;
+          c->wpb = wpb0;
+        } else {
+          break;
+        }
       }
     }
     if (bps <= 0) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "async kernel does not fit on an SM");
@@ -303,7 +313,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     c->long_visit = p.long_visit > 0 ? p.long_visit : 14;
     // columns whose serial chain is long enough to set the epoch time skip the queue
     int64_t pri_min = 0;
-    if (!p.exact && p.priority_permille >= 0) {
+    if (cta_heavy) {
       const int permille = p.priority_permille > 0 ? p.priority_permille : 50;
       pri_min = std::max<int64_t>(1, c->max_column * permille / 1000);
     }

@@ -109,9 +109,9 @@ def test_async_one_worker_close_to_replay(ng, O, gpu_ok, long_visit):
 
 
 @pytest.mark.parametrize("wpb,dim,precision", [(1, 32, "fp32"), (3, 100, "fp32"), (8, 100, "fp32"),
-                                               (8, 7, "fp32"), (8, 200, "fp32"), (14, 100, "fp32"),
+                                               (8, 7, "fp32"), (8, 200, "fp32"), (10, 100, "fp32"),
                                                (8, 100, "bf16"), (3, 7, "bf16"), (8, 200, "bf16"),
-                                               (14, 100, "bf16")])
+                                               (12, 100, "bf16")])
 def test_block_visits_close_to_replay(ng, O, gpu_ok, wpb, dim, precision):
     """Every column on the priority route and one thread block of `wpb` warps: each visit
     is a whole column, processed by the block's warps together in blocks of 32 ratings

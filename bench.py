@@ -7,8 +7,8 @@ planted rank-20 model), k = 100, lrate 0.002, drate 0.05, reg 0.05: seeded synth
 data with the shape of the Netflix-prize matrix (the dataset itself is not used).
 
 One step = one epoch of the async NOMAD kernel: every training rating updated once,
-column tokens passed between worker warps (14 per thread block, one block per SM: 2,128
-workers) through device ring queues; columns long enough to set the epoch time visit
+column tokens passed between worker warps (one block per SM with 12 worker warps for bf16
+rows, 10 for fp32: 1,824 / 1,520 workers) through device ring queues; columns long enough to set the epoch time visit
 whole thread blocks.  Both storage
 forms run (fp32 and bf16 with stochastic rounding); the headline value is the bf16
 form.  The device-resident number (`value`) sums CUDA-event time of the K timed epoch

@@ -113,6 +113,10 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
   out.n = n;
   out.col_ptr.assign(static_cast<size_t>(n) + 1, 0);
   out.ratings.resize(static_cast<size_t>(nnz));
+  out.row_nnz.resize(static_cast<size_t>(m));
+  parallel_chunks(m, threads, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) out.row_nnz[i] = static_cast<int32_t>(R.row_ptr[i + 1] - R.row_ptr[i]);
+  });
   if (nnz == 0) return NOMAD_OK;
   // Stable counting sort by column: contiguous chunks of the row-major entries, one
   // column histogram per chunk, then each chunk scatters in order.
@@ -173,21 +177,25 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     const int64_t per = m / P + ((m % P > 0) ? 1 : 0);
     for (int32_t w = 0; w <= P; ++w) L.row_start[w] = static_cast<int32_t>(std::min<int64_t>(per * w, m));
   } else {
-    // contiguous blocks holding ~nnz/P ratings each; ratings per row from per-thread
-    // histograms (no shared counters)
-    const int nt = std::max(1, std::min<int>(threads, 64));
-    std::vector<std::vector<int32_t>> part(static_cast<size_t>(nt));
-    parallel_chunks(nnz, nt, [&](int t, int64_t lo, int64_t hi) {
-      std::vector<int32_t>& h = part[static_cast<size_t>(t)];
-      h.assign(static_cast<size_t>(m), 0);
-      for (int64_t o = lo; o < hi; ++o) ++h[csc.ratings[o].row];
-    });
-    std::vector<int32_t> row_nnz(m, 0);
-    parallel_chunks(m, nt, [&](int, int64_t lo, int64_t hi) {
-      for (const auto& h : part)
-        if (!h.empty())
-          for (int64_t i = lo; i < hi; ++i) row_nnz[i] += h[i];
-    });
+    // contiguous blocks holding ~nnz/P ratings each; ratings per row as build_csc
+    // counted them, else from per-thread histograms (no shared counters)
+    std::vector<int32_t> counted;
+    if (csc.row_nnz.size() != static_cast<size_t>(m)) {
+      const int nt = std::max(1, std::min<int>(threads, 64));
+      std::vector<std::vector<int32_t>> part(static_cast<size_t>(nt));
+      parallel_chunks(nnz, nt, [&](int t, int64_t lo, int64_t hi) {
+        std::vector<int32_t>& h = part[static_cast<size_t>(t)];
+        h.assign(static_cast<size_t>(m), 0);
+        for (int64_t o = lo; o < hi; ++o) ++h[csc.ratings[o].row];
+      });
+      counted.assign(static_cast<size_t>(m), 0);
+      parallel_chunks(m, nt, [&](int, int64_t lo, int64_t hi) {
+        for (const auto& h : part)
+          if (!h.empty())
+            for (int64_t i = lo; i < hi; ++i) counted[i] += h[i];
+      });
+    }
+    const std::vector<int32_t>& row_nnz = counted.empty() ? csc.row_nnz : counted;
     int64_t acc = 0;
     int32_t w = 1;
     L.row_start[0] = 0;

@@ -1,8 +1,12 @@
 // layout.h -- host-side construction of the device data layout.
 #pragma once
 
+#include <sys/mman.h>
+
 #include <cstdint>
+#include <cstdlib>
 #include <memory>
+#include <new>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -19,16 +23,33 @@ struct Rating {
 
 // Allocator whose value construction leaves trivial elements uninitialised, so that
 // resize() of a large buffer that is filled next writes no zeros first (the first touch
-// of its pages then happens in the parallel fill).
+// of its pages then happens in the parallel fill).  Buffers of 32 MB and more are
+// 2 MB-aligned and advised for transparent huge pages: fewer page faults on first touch.
 template <typename T>
 struct NoInitAllocator : std::allocator<T> {
   template <typename U>
   struct rebind {
     using other = NoInitAllocator<U>;
   };
+  static constexpr size_t kHugeBytes = size_t{32} << 20;
   NoInitAllocator() = default;
   template <typename U>
   NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+  T* allocate(size_t count) {
+    const size_t bytes = count * sizeof(T);
+    if (bytes < kHugeBytes) return std::allocator<T>::allocate(count);
+    void* p = nullptr;
+    if (posix_memalign(&p, size_t{2} << 20, bytes) != 0) throw std::bad_alloc();
+    madvise(p, bytes, MADV_HUGEPAGE);  // advice only: ignored where huge pages are off
+    return static_cast<T*>(p);
+  }
+  void deallocate(T* p, size_t count) noexcept {
+    if (count * sizeof(T) < kHugeBytes) {
+      std::allocator<T>::deallocate(p, count);
+      return;
+    }
+    std::free(p);
+  }
   template <typename U>
   void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) {
     ::new (static_cast<void*>(p)) U;
@@ -45,6 +66,7 @@ struct Csc {
   int32_t m = 0, n = 0;
   std::vector<int64_t> col_ptr;  // [n+1]
   std::vector<Rating, NoInitAllocator<Rating>> ratings;  // [nnz]
+  std::vector<int32_t> row_nnz;  // [m] ratings per row (from the row-major input)
   int64_t nnz() const { return col_ptr.empty() ? 0 : col_ptr.back(); }
 };
 
@@ -61,7 +83,7 @@ struct AsyncLayout {
   int32_t P = 0;
   std::vector<int32_t> row_start;  // [P+1] first row of each worker's block
   std::vector<int64_t> vl_ptr;     // [n+1] visit list of each column
-  std::vector<Segment> segs;       // visits, each column's list in its route order
+  std::vector<Segment, NoInitAllocator<Segment>> segs;  // visits, each column's list in its route order
   std::vector<int32_t> qnext0;     // [n+2P] initial queues (tokens in column order)
   std::vector<int32_t> qtail0;     // [2P]: queue w = worker w's queue, P+w its priority queue
   std::vector<int32_t> desc0;      // [4n] first visit of each token {start lo, hi, len, 0|heavy}

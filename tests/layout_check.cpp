@@ -1,0 +1,156 @@
+// Invariants of the host-side layout (nomad_gb300/csrc/host_layout.cpp) on seeded
+// random matrices, on the CPU: the CSC holds every rating once, columns ascending by
+// row, with the row counts of the input; the worker row blocks are contiguous and cover
+// every row; a column's visits cover its ratings exactly once, each visit a run of rows
+// owned by one worker (or one group of `group` workers for a priority column); routes
+// that keep a group's visits consecutive do so; every active token starts in exactly one
+// queue, at a rank below that queue's count.  Prints "layout ok" and exits 0 when all
+// cases hold.
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <set>
+#include <vector>
+
+#include "layout.h"
+
+namespace {
+
+int g_fail = 0;
+#define CHECK(c)                                                             \
+  do {                                                                       \
+    if (!(c)) {                                                              \
+      std::printf("FAIL line %d: %s\n", __LINE__, #c);                       \
+      if (++g_fail > 20) return;                                             \
+    }                                                                        \
+  } while (0)
+
+uint64_t g_s = 0x243F6A8885A308D3ull;
+uint32_t next_u32() {
+  g_s ^= g_s << 13;
+  g_s ^= g_s >> 7;
+  g_s ^= g_s << 17;
+  return static_cast<uint32_t>(g_s >> 11);
+}
+
+// m x n with about `per_row` distinct columns per row, skewed towards low column ids.
+void run_case(int32_t m, int32_t n, int per_row, int32_t P, int balance, int64_t pri_min, int32_t group,
+              bool group_routes, int threads) {
+  std::vector<int32_t> rc(m), cols;
+  std::vector<float> vals;
+  for (int32_t i = 0; i < m; ++i) {
+    std::set<int32_t> cs;
+    const int k = static_cast<int>(next_u32() % (2 * per_row + 1));
+    while (static_cast<int>(cs.size()) < std::min(k, n)) {
+      const uint32_t a = next_u32() % n, b = next_u32() % n;
+      cs.insert(static_cast<int32_t>(std::min(a, b)));  // skew: more ratings in low columns
+    }
+    rc[i] = static_cast<int32_t>(cs.size());
+    for (int32_t c : cs) {
+      cols.push_back(c);
+      vals.push_back(static_cast<float>(1 + next_u32() % 5));
+    }
+  }
+  const int64_t nnz = static_cast<int64_t>(cols.size());
+  nomad_gpu_matrix A{nnz, rc.data(), nullptr, cols.data(), nullptr, vals.data()};
+  nomad::Csc csc;
+  CHECK(nomad::build_csc(A, m, n, csc, threads) == 0);
+  CHECK(csc.nnz() == nnz);
+  CHECK(csc.row_nnz.size() == static_cast<size_t>(m));
+  for (int32_t i = 0; i < m && i < static_cast<int32_t>(csc.row_nnz.size()); ++i) CHECK(csc.row_nnz[i] == rc[i]);
+  std::vector<int32_t> seen_per_row(m, 0);
+  for (int32_t j = 0; j < n; ++j)
+    for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
+      if (o > csc.col_ptr[j]) CHECK(csc.ratings[o].row > csc.ratings[o - 1].row);
+      ++seen_per_row[csc.ratings[o].row];
+    }
+  CHECK(seen_per_row == rc);
+
+  for (int with_counts = 0; with_counts < 2; ++with_counts) {
+    nomad::Csc c2;
+    const nomad::Csc* cp = &csc;
+    if (!with_counts) {  // the same layout without the row counts (per-thread histograms)
+      c2.m = csc.m;
+      c2.n = csc.n;
+      c2.col_ptr = csc.col_ptr;
+      c2.ratings = csc.ratings;
+      cp = &c2;
+    }
+    nomad::AsyncLayout L;
+    CHECK(nomad::build_async_layout(*cp, P, balance, 12345, pri_min, group, group_routes, L, threads) == 0);
+    CHECK(L.row_start.size() == static_cast<size_t>(P) + 1);
+    CHECK(L.row_start[0] == 0 && L.row_start[P] == m);
+    for (int32_t w = 0; w < P; ++w) CHECK(L.row_start[w] <= L.row_start[w + 1]);
+    std::vector<int32_t> owner(m);
+    for (int32_t w = 0; w < P; ++w)
+      for (int32_t r = L.row_start[w]; r < L.row_start[w + 1]; ++r) owner[r] = w;
+    int64_t covered = 0, n_pri = 0, n_active = 0;
+    std::vector<int32_t> qcount(2 * static_cast<size_t>(P), 0);
+    for (int32_t j = 0; j < n; ++j) {
+      const int64_t len = csc.col_ptr[j + 1] - csc.col_ptr[j];
+      const bool pri = pri_min > 0 && len >= pri_min;
+      n_pri += pri && len > 0;
+      std::vector<int64_t> starts;
+      std::set<int32_t> targets;
+      int32_t prev_group = -1;
+      std::set<int32_t> closed_groups;
+      for (int64_t v = L.vl_ptr[j]; v < L.vl_ptr[j + 1]; ++v) {
+        const nomad::Segment& sg = L.segs[v];
+        CHECK(sg.len > 0);
+        CHECK(sg.start >= csc.col_ptr[j] && sg.start + sg.len <= csc.col_ptr[j + 1]);
+        starts.push_back(sg.start);
+        covered += sg.len;
+        for (int64_t o = sg.start; o < sg.start + sg.len; ++o) {
+          const int32_t w = owner[csc.ratings[o].row];
+          CHECK((pri ? w / group : w) == sg.worker);
+        }
+        CHECK(targets.insert(sg.worker).second);  // one visit per owner
+        if (group_routes && !pri && group > 1) {  // a group's visits stay consecutive
+          const int32_t g = sg.worker / group;
+          if (g != prev_group) {
+            CHECK(closed_groups.count(g) == 0);
+            if (prev_group >= 0) closed_groups.insert(prev_group);
+            prev_group = g;
+          }
+        }
+      }
+      std::sort(starts.begin(), starts.end());  // the visits tile the column
+      int64_t pos = csc.col_ptr[j];
+      for (int64_t st : starts) {
+        CHECK(st == pos);
+        int64_t l = 0;
+        for (int64_t v = L.vl_ptr[j]; v < L.vl_ptr[j + 1]; ++v)
+          if (L.segs[v].start == st) l = L.segs[v].len;
+        pos += l;
+      }
+      CHECK(pos == csc.col_ptr[j + 1]);
+      const int32_t q = L.first_q[2 * static_cast<size_t>(j)], rank = L.first_q[2 * static_cast<size_t>(j) + 1];
+      if (len == 0) {
+        CHECK(q == -1);
+        continue;
+      }
+      ++n_active;
+      const nomad::Segment& s0 = L.segs[L.vl_ptr[j]];
+      CHECK(q == (pri ? P : 0) + s0.worker);
+      CHECK(rank == qcount[q]++);
+    }
+    CHECK(covered == nnz);
+    CHECK(L.n_active == n_active);
+    CHECK(L.n_priority == n_pri);
+    for (size_t q = 0; q < qcount.size(); ++q) CHECK(L.q_count[q] == qcount[q]);
+  }
+}
+
+}  // namespace
+
+int main() {
+  // m, n, ratings per row, workers, balance, priority threshold, group, group routes, threads
+  run_case(3000, 200, 12, 64, 1, 0, 1, false, 4);
+  run_case(3000, 200, 12, 64, 0, 0, 1, false, 3);
+  run_case(5000, 300, 20, 60, 1, 150, 12, true, 8);
+  run_case(5000, 300, 20, 40, 1, 100, 10, true, 1);
+  run_case(400, 50, 5, 7, 1, 30, 3, true, 2);
+  run_case(17, 9, 3, 30, 1, 0, 1, false, 4);  // more workers than rows
+  std::printf("%s\n", g_fail ? "layout FAILED" : "layout ok");
+  return g_fail ? 1 : 0;
+}

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "common.h"
@@ -244,27 +245,43 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   if (p.init == NOMAD_INIT_HASH && !(prob->W0 && prob->H0)) {
     CK(nomad::launch_init_hash(f, p.seed, c->stream));
   }
-  if (prob->W0) {
-    RC(put_factor(c, f.W, prob->W0, f.m));
-  } else if (p.init != NOMAD_INIT_HASH) {
-    std::vector<float> Wh(static_cast<size_t>(f.m) * f.dim);
-    RC(nomad_reference_init(f.m, 0, f.dim, p.seed, p.init_parts, Wh.data(), nullptr));
-    RC(put_factor(c, f.W, Wh.data(), f.m));
-  }
-  if (prob->H0) {
-    RC(put_factor(c, f.H, prob->H0, f.n));
-  } else if (p.init != NOMAD_INIT_HASH) {
-    std::vector<float> Hh(static_cast<size_t>(f.n) * f.dim);
-    RC(nomad_reference_init(0, f.n, f.dim, p.seed, p.init_parts, nullptr, Hh.data()));
-    RC(put_factor(c, f.H, Hh.data(), f.n));
-  }
-
-  trace.mark("factors (init + upload)", c->stream);
+  // The reference init of W (parallel over its row parts) and of H (one sequential stream)
+  // runs on two threads beside the CSC builds; the uploads follow.
+  const bool host_w = !prob->W0 && p.init != NOMAD_INIT_HASH;
+  const bool host_h = !prob->H0 && p.init != NOMAD_INIT_HASH;
+  std::vector<float, nomad::NoInitAllocator<float>> Wh(host_w ? static_cast<size_t>(f.m) * f.dim : 0);
+  std::vector<float, nomad::NoInitAllocator<float>> Hh(host_h ? static_cast<size_t>(f.n) * f.dim : 0);
+  int rc_w = NOMAD_OK, rc_h = NOMAD_OK;
+  std::thread tw, th;
+  struct Join {  // no early return leaves a running thread behind
+    std::thread& a;
+    std::thread& b;
+    ~Join() {
+      if (a.joinable()) a.join();
+      if (b.joinable()) b.join();
+    }
+  } join{tw, th};
+  if (host_w) tw = std::thread([&] { rc_w = nomad_reference_init(f.m, 0, f.dim, p.seed, p.init_parts, Wh.data(), nullptr); });
+  if (host_h) th = std::thread([&] { rc_h = nomad_reference_init(0, f.n, f.dim, p.seed, p.init_parts, nullptr, Hh.data()); });
   // ---- rating sets ---------------------------------------------------------------
   nomad::Csc train, test;
   RC(nomad::build_csc(prob->train, f.m, f.n, train, threads));
   RC(nomad::build_csc(prob->test, f.m, f.n, test, threads));
-  trace.mark("CSC build");
+  trace.mark("CSC build (factor init beside it)");
+  if (tw.joinable()) tw.join();
+  if (th.joinable()) th.join();
+  if (rc_w != NOMAD_OK || rc_h != NOMAD_OK) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "reference init of the factors failed");
+  if (prob->W0) {
+    RC(put_factor(c, f.W, prob->W0, f.m));
+  } else if (host_w) {
+    RC(put_factor(c, f.W, Wh.data(), f.m));
+  }
+  if (prob->H0) {
+    RC(put_factor(c, f.H, prob->H0, f.n));
+  } else if (host_h) {
+    RC(put_factor(c, f.H, Hh.data(), f.n));
+  }
+  trace.mark("factors (init wait + upload)", c->stream);
   c->nnz_train = train.nnz();
   c->nnz_test = test.nnz();
   RC(upload_csc(c, train, &c->train, &c->train_ptr));

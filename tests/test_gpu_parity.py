@@ -303,3 +303,28 @@ def test_factor_roundtrip(ng, gpu_ok):
         nm.set_factors(W, H)
         W3, _ = nm.factors()
     assert np.max(np.abs(W3 - W) / np.maximum(np.abs(W), 1e-6)) <= 2 ** -8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_async_block_size_and_wide_rows(ng, gpu_ok, precision):
+    """The pipelined kernel is compiled for 10 compute warps per block with fp32 rows and
+    12 with bf16 rows (plus the pop and push warps); a request for more is capped, and
+    rows of 512 values (where block visits may not fit shared memory beside the warps'
+    staging rings and are then switched off) still train every rating once per epoch."""
+    train, test = small_problem(ng, m=3000, n=300, nnz_train=60000, nnz_test=2000)
+    cap = 10 if precision == "fp32" else 12
+    with ng.Nomad(train, test, dim=32, lrate=LR, drate=DR, reg=REG, mode="async", precision=precision,
+                  warps_per_block=14) as nm:
+        info = nm.info()
+        st = nm.epoch(2)
+    assert info["block_threads"] == (cap + 2) * 32
+    assert (info["grid_blocks"] - 1) * cap < info["workers"] <= info["grid_blocks"] * cap
+    assert st["updates"] == 2 * train.nnz
+    rm = []
+    with ng.Nomad(train, test, dim=512, lrate=LR, drate=DR, reg=REG, mode="async", precision=precision) as nm:
+        for _ in range(3):
+            st = nm.epoch(1)
+            assert st["updates"] == train.nnz
+            rm.append(nm.rmse()[1])
+    assert all(np.isfinite(rm)) and rm[-1] < rm[0], rm

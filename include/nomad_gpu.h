@@ -237,6 +237,28 @@ int nomad_gpu_device_ok(int32_t device);
  * column chains set the epoch time.  NOMAD_ERR_UNSUPPORTED in other modes. */
 int nomad_gpu_token_finish_times(nomad_gpu_ctx* ctx, double* seconds);
 
+/* ---- autotuning of the ASYNC kernel ------------------------------------------------
+ * One configuration tried by nomad_gpu_autotune and its mean device time per epoch. */
+typedef struct nomad_gpu_tune_trial {
+  int32_t warps_per_block;   /* compute warps per thread block                          */
+  int32_t priority_permille; /* priority threshold (negative: no priority queues)       */
+  int32_t long_visit;        /* visits this long or longer take the blocked path        */
+  int32_t status;            /* NOMAD_OK, or the status the trial ended with            */
+  double device_ms;          /* mean device time of the timed epochs                    */
+} nomad_gpu_tune_trial;
+
+/* Chooses the runtime configuration of the ASYNC (non-exact) kernel for this problem by
+ * measurement: coordinate descent over warps per block (the compiled maximum and two
+ * and four fewer), then the priority threshold (25, 50, 100 permille, off), then the
+ * long-visit length (10, 14, 20).  Each trial is a fresh context from params (the same
+ * initial factors every time), one untimed epoch and `epochs` timed ones; the factors it
+ * trains are discarded.  On success *params holds the fastest configuration (the other
+ * fields unchanged) and trials[0 .. *n_trials) the measurements (at most max_trials are
+ * stored; trials may be NULL when max_trials is 0).  NOMAD_ERR_UNSUPPORTED for other
+ * modes and for exact = 1. */
+int nomad_gpu_autotune(const nomad_gpu_problem* prob, nomad_gpu_params* params, int32_t epochs,
+                       nomad_gpu_tune_trial* trials, int32_t max_trials, int32_t* n_trials);
+
 /* ---- evaluation without device allocation ---------------------------------------
  * No counterpart in the reference: it is an extra entry point for callers that
  * cannot obtain device memory from the CUDA allocator -- a host runtime that hands

@@ -200,6 +200,26 @@ def device_ok(device=0):
     return bool(lib().nomad_gpu_device_ok(device))
 
 
+def autotune(train, test=None, epochs=1, W0=None, H0=None, **kw):
+    """Measured choice of the ASYNC kernel's runtime configuration for this problem
+    (nomad_gpu_autotune): returns (keyword arguments for Nomad with warps_per_block,
+    priority_permille and long_visit set, list of the trials with their ms per epoch)."""
+    p = default_params(**kw)
+    if test is None:
+        test = RatingMatrix(train.m, train.n, np.zeros(train.m, np.int32),
+                            np.zeros(0, np.int32), np.zeros(0))
+    W0 = None if W0 is None else np.ascontiguousarray(W0, np.float32)
+    H0 = None if H0 is None else np.ascontiguousarray(H0, np.float32)
+    prob = _abi.Problem(train.m, train.n, train._c(), test._c(), _ptr(W0), _ptr(H0))
+    trials = (_abi.TuneTrial * 32)()
+    n = ctypes.c_int32()
+    check(lib().nomad_gpu_autotune(ctypes.byref(prob), ctypes.byref(p), epochs, trials, 32, ctypes.byref(n)),
+          "nomad_gpu_autotune")
+    best = dict(kw, warps_per_block=p.warps_per_block, priority_permille=p.priority_permille,
+                long_visit=p.long_visit)
+    return best, [{k: getattr(t, k) for k, _ in _abi.TuneTrial._fields_} for t in trials[:n.value]]
+
+
 class Nomad:
     """One training context on the GPU (nomad_gpu_ctx)."""
 

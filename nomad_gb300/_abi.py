@@ -69,6 +69,11 @@ class EpochStats(ctypes.Structure):
                 ("lrate", c_dbl)]
 
 
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("warps_per_block", c_i32), ("priority_permille", c_i32), ("long_visit", c_i32),
+                ("status", c_i32), ("device_ms", c_dbl)]
+
+
 class CheckpointInfo(ctypes.Structure):
     _fields_ = [("m", c_i32), ("n", c_i32), ("dim", c_i32), ("epochs_done", c_i32),
                 ("lrate", c_dbl), ("objective", c_dbl)]
@@ -121,6 +126,8 @@ SIGNATURES = {
     "nomad_gpu_last_error": (ctypes.c_char_p, []),
     "nomad_gpu_device_ok": (ctypes.c_int, [c_i32]),
     "nomad_gpu_token_finish_times": (ctypes.c_int, [c_vp, c_vp]),
+    "nomad_gpu_autotune": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params), c_i32,
+                                          ctypes.POINTER(TuneTrial), c_i32, ctypes.POINTER(c_i32)]),
     "nomad_gpu_sse_noalloc": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,
                                              c_i64, c_i32, c_vp, c_vp]),
     "nomad_gpu_batch_init": (ctypes.c_int, [ctypes.POINTER(c_vp), ctypes.POINTER(BatchProblem), c_i32,

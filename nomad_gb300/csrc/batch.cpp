@@ -124,7 +124,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, b->device));
   if (prop.major * 10 + prop.minor != 103)
-    NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", b->device, prop.major,
+    NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device %d is sm_%d%d; the library is compiled for sm_103a", b->device, prop.major,
                prop.minor);
   b->num_sms = prop.multiProcessorCount;
   CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

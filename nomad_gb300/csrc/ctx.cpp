@@ -213,7 +213,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, c->device));
   if (prop.major * 10 + prop.minor != 103)
-    NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", c->device,
+    NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device %d is sm_%d%d; the library is compiled for sm_103a", c->device,
                prop.major, prop.minor);
   if (!prop.cooperativeLaunch) NOMAD_FAIL(NOMAD_ERR_NO_DEVICE, "device lacks cooperative launch");
   c->num_sms = prop.multiProcessorCount;
@@ -866,6 +866,89 @@ const char* nomad_gpu_strerror(int status) {
 }
 
 const char* nomad_gpu_last_error(void) { return nomad::last_error(); }
+
+int nomad_gpu_autotune(const nomad_gpu_problem* prob, nomad_gpu_params* params, int32_t epochs,
+                       nomad_gpu_tune_trial* trials, int32_t max_trials, int32_t* n_trials) {
+  nomad::clear_last_error();
+  if (!prob || !params || epochs < 1 || max_trials < 0 || (max_trials > 0 && !trials))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_gpu_autotune");
+  if (params->mode != NOMAD_MODE_ASYNC || params->exact)
+    NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "autotuning covers the ASYNC kernel (exact = 0)");
+  if (n_trials) *n_trials = 0;
+  std::vector<nomad_gpu_tune_trial> done;
+  // one trial: a fresh context, an untimed epoch, `epochs` timed ones
+  auto run = [&](int32_t wpb, int32_t pri, int32_t lv) -> double {
+    for (const auto& t : done)
+      if (t.warps_per_block == wpb && t.priority_permille == pri && t.long_visit == lv)
+        return t.status == NOMAD_OK ? t.device_ms : -1.0;
+    nomad_gpu_params q = *params;
+    q.warps_per_block = wpb;
+    q.priority_permille = pri;
+    q.long_visit = lv;
+    nomad_gpu_tune_trial t{wpb, pri, lv, NOMAD_OK, -1.0};
+    nomad_gpu_ctx* c = nullptr;
+    t.status = nomad_gpu_init(&c, prob, &q);
+    if (t.status == NOMAD_OK) {
+      nomad_gpu_epoch_stats st;
+      t.status = nomad_gpu_epoch(c, 1, &st);
+      double ms = 0;
+      for (int32_t e = 0; e < epochs && t.status == NOMAD_OK; ++e) {
+        t.status = nomad_gpu_epoch(c, 1, &st);
+        ms += st.device_ms;
+      }
+      if (t.status == NOMAD_OK) {
+        nomad_gpu_info info;
+        nomad_gpu_get_info(c, &info);
+        t.warps_per_block = info.block_threads / 32 - 2;  // what the kernel ran with
+        t.device_ms = ms / epochs;
+      }
+    }
+    nomad_gpu_destroy(c);
+    done.push_back(t);
+    return t.status == NOMAD_OK ? t.device_ms : -1.0;
+  };
+  auto better = [](double a, double b) { return a >= 0 && (b < 0 || a < b); };
+  // warps per block: the compiled maximum (what 0 resolves to), then fewer
+  int32_t pri = params->priority_permille == 0 ? 50 : params->priority_permille;  // the defaults, spelt out
+  int32_t lv = params->long_visit > 0 ? params->long_visit : 14;
+  double best = run(0, pri, lv);
+  const int32_t cap = done.empty() || done.back().status != NOMAD_OK ? 0 : done.back().warps_per_block;
+  int32_t wpb = cap;
+  for (int32_t w : {cap - 2, cap - 4}) {
+    if (w < 1) continue;
+    const double ms = run(w, pri, lv);
+    if (better(ms, best)) {
+      best = ms;
+      wpb = w;
+    }
+  }
+  for (int32_t p : {25, 50, 100, -1}) {
+    const double ms = run(wpb, p, lv);
+    if (better(ms, best)) {
+      best = ms;
+      pri = p;
+    }
+  }
+  for (int32_t l : {10, 14, 20}) {
+    const double ms = run(wpb, pri, l);
+    if (better(ms, best)) {
+      best = ms;
+      lv = l;
+    }
+  }
+  const int32_t stored = std::min<int32_t>(max_trials, static_cast<int32_t>(done.size()));
+  for (int32_t i = 0; i < stored; ++i) trials[i] = done[i];
+  if (n_trials) *n_trials = stored;
+  if (best < 0) {
+    const int32_t st = done.empty() ? NOMAD_ERR_INVALID_ARG : done.front().status;
+    NOMAD_FAIL(st, "no configuration completed an epoch");
+  }
+  params->warps_per_block = wpb;
+  params->priority_permille = pri;
+  params->long_visit = lv;
+  nomad::clear_last_error();  // a trial that failed left its detail behind
+  return NOMAD_OK;
+}
 
 int nomad_gpu_token_finish_times(nomad_gpu_ctx* c, double* seconds) {
   nomad::clear_last_error();

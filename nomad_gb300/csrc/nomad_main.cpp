@@ -60,7 +60,7 @@ struct Options {
   int verbose = 0;
   // GPU options
   std::string mode = "async", precision = "fp32", lr_strategy = "fixed";
-  int epochs = 0, workers = 0, device = 0, exact = 0, dsgd_blocks = 0;
+  int epochs = 0, workers = 0, device = 0, exact = 0, dsgd_blocks = 0, autotune = 0;
   std::string init = "reference";
 };
 
@@ -106,6 +106,8 @@ const char* kUsage =
     "  --workers arg (=0)           async worker warps (0 = all resident)\n"
     "  --dsgd_blocks arg (=0)       DSGD blocks per side (0 = auto)\n"
     "  --exact arg (=0)             reference operation order\n"
+    "  --autotune arg (=0)          async: first measure configurations, this many timed\n"
+    "                               epochs each, and train with the fastest\n"
     "  --init arg (=reference)      reference | hash\n"
     "  --device arg (=0)            CUDA device\n";
 
@@ -215,6 +217,7 @@ bool parse(int argc, char** argv, Options& o, bool& help) {
       else if (name == "device") o.device = std::stoi(v);
       else if (name == "exact") o.exact = std::stoi(v);
       else if (name == "dsgd_blocks") o.dsgd_blocks = std::stoi(v);
+      else if (name == "autotune") o.autotune = std::stoi(v);
       else if (name == "init") o.init = v;
       else {
         std::cerr << "error: unrecognised option '--" << name << "'\n";
@@ -294,6 +297,27 @@ int main(int argc, char** argv) {
   prob.n = train.n;
   prob.train = nomad_gpu_matrix{train.nnz, train.row_counts, nullptr, train.cols, train.vals, nullptr};
   prob.test = nomad_gpu_matrix{test.nnz, test.row_counts, nullptr, test.cols, test.vals, nullptr};
+  if (o.autotune > 0 && prm.mode == NOMAD_MODE_ASYNC && !prm.exact) {
+    nomad_gpu_tune_trial trials[32];
+    int32_t nt = 0;
+    rc = nomad_gpu_autotune(&prob, &prm, o.autotune, trials, 32, &nt);
+    if (rc) {
+      std::cerr << "nomad_gpu_autotune: " << nomad_gpu_strerror(rc) << ": " << nomad_gpu_last_error() << "\n";
+      return 1;
+    }
+    double best = -1;
+    for (int32_t i = 0; i < nt; ++i) {
+      std::cerr << "M: autotune trial: warps per block " << trials[i].warps_per_block << ", priority "
+                << trials[i].priority_permille << " permille, long visit " << trials[i].long_visit << ": "
+                << trials[i].device_ms << " ms per epoch\n";
+      if (trials[i].status == NOMAD_OK && trials[i].warps_per_block == prm.warps_per_block &&
+          trials[i].priority_permille == prm.priority_permille && trials[i].long_visit == prm.long_visit)
+        best = trials[i].device_ms;
+    }
+    std::cerr << "M: autotune: warps per block " << prm.warps_per_block << ", priority "
+              << prm.priority_permille << " permille, long visit " << prm.long_visit << " (" << best
+              << " ms per epoch)\n";
+  }
   nomad_gpu_ctx* ctx = nullptr;
   rc = nomad_gpu_init(&ctx, &prob, &prm);
   if (rc) {

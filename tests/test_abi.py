@@ -37,6 +37,7 @@ def test_struct_sizes_match_headers(ng):
     assert ctypes.sizeof(ng._abi.Matrix) == 48
     assert ctypes.sizeof(ng._abi.EpochStats) == 8 * 3 + 4 * 2 + 8 * 5
     assert ctypes.sizeof(ng._abi.CheckpointInfo) == 32
+    assert ctypes.sizeof(ng._abi.TuneTrial) == 24
 
 
 def test_defaults_are_the_references(ng):

@@ -1,0 +1,36 @@
+"""nomad_gpu_autotune: the measured choice of the ASYNC kernel's runtime configuration
+(warps per block, priority threshold, long-visit length) by coordinate descent over fresh
+contexts.  Checked: the trials it reports ran, the configuration it returns is the
+fastest of them, training with it updates every rating, and other modes are refused."""
+import pytest
+
+from test_gpu_parity import LR, DR, REG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_autotune_picks_the_fastest_trial(ng, gpu_ok, precision):
+    train, test = ng.synth(ng.synth_spec(2, m=20000, n=1000, nnz_train=400000, nnz_test=20000, seed=12345))
+    kw = dict(dim=32, lrate=LR, drate=DR, reg=REG, mode="async", precision=precision)
+    best, trials = ng.autotune(train, test, epochs=1, **kw)
+    cap = 10 if precision == "fp32" else 12
+    assert len(trials) >= 6
+    assert all(t["status"] == 0 and t["device_ms"] > 0 for t in trials)
+    assert {t["warps_per_block"] for t in trials} <= {cap, cap - 2, cap - 4}
+    assert {t["priority_permille"] for t in trials} >= {25, 50, 100, -1}
+    assert {t["long_visit"] for t in trials} >= {10, 14, 20}
+    fastest = min(trials, key=lambda t: t["device_ms"])
+    chosen = [t for t in trials if (t["warps_per_block"], t["priority_permille"], t["long_visit"]) ==
+              (best["warps_per_block"], best["priority_permille"], best["long_visit"])]
+    assert chosen and chosen[0]["device_ms"] == fastest["device_ms"]
+    with ng.Nomad(train, test, **best) as nm:
+        assert nm.epoch(1)["updates"] == train.nnz
+
+
+@pytest.mark.gpu
+def test_autotune_refuses_other_modes(ng, gpu_ok):
+    train, test = ng.synth(ng.synth_spec(2, m=2000, n=200, nnz_train=20000, nnz_test=1000, seed=12345))
+    for kw in (dict(mode="dsgd"), dict(mode="replay"), dict(mode="async", exact=1)):
+        with pytest.raises(ng.NomadError) as e:
+            ng.autotune(train, test, dim=16, **kw)
+        assert e.value.status == -9

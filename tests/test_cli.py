@@ -191,3 +191,16 @@ def test_recover_keeps_the_bold_driver_rate(ng, gpu_ok, tmp_path):
     r2 = run(*common, "--epochs", "3", "--output", str(tmp_path / "straight"))
     assert r2.returncode == 0, r2.stderr
     assert open(tmp_path / "resumed0").read() == open(tmp_path / "straight0").read()
+
+
+@pytest.mark.gpu
+def test_autotune_option(ng, gpu_ok, tmp_path):
+    """--autotune N measures the async kernel's configurations (N timed epochs each),
+    reports each trial and the choice, then trains with it."""
+    _write_dataset(ng, str(tmp_path))
+    r = run("--path", str(tmp_path), "--dim", "8", "--epochs", "1", "--pause", "0", "--autotune", "1",
+            "--timeout", "1")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stderr.count("M: autotune trial:") >= 6
+    assert "M: autotune: warps per block" in r.stderr
+    assert "current test RMSE" in r.stdout

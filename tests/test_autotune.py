@@ -27,10 +27,13 @@ def test_autotune_picks_the_fastest_trial(ng, gpu_ok, precision):
         assert nm.epoch(1)["updates"] == train.nnz
 
 
-@pytest.mark.gpu
-def test_autotune_refuses_other_modes(ng, gpu_ok):
+def test_autotune_refuses_other_modes(ng):
+    """Checked before any device work, so this runs without a GPU."""
     train, test = ng.synth(ng.synth_spec(2, m=2000, n=200, nnz_train=20000, nnz_test=1000, seed=12345))
     for kw in (dict(mode="dsgd"), dict(mode="replay"), dict(mode="async", exact=1)):
         with pytest.raises(ng.NomadError) as e:
             ng.autotune(train, test, dim=16, **kw)
         assert e.value.status == -9
+    with pytest.raises(ng.NomadError) as e:
+        ng.autotune(train, test, epochs=0, dim=16)
+    assert e.value.status == -1

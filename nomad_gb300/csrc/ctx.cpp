@@ -14,6 +14,7 @@
 #include "common.h"
 #include "launch.h"
 #include "trace.h"
+#include "tune.h"
 #include "layout.h"
 
 using nomad::DevFactors;
@@ -877,15 +878,11 @@ int nomad_gpu_autotune(const nomad_gpu_problem* prob, nomad_gpu_params* params, 
   if (n_trials) *n_trials = 0;
   std::vector<nomad_gpu_tune_trial> done;
   // one trial: a fresh context, an untimed epoch, `epochs` timed ones
-  auto run = [&](int32_t wpb, int32_t pri, int32_t lv) -> double {
-    for (const auto& t : done)
-      if (t.warps_per_block == wpb && t.priority_permille == pri && t.long_visit == lv)
-        return t.status == NOMAD_OK ? t.device_ms : -1.0;
+  auto measure = [&](nomad_gpu_tune_trial& t) {
     nomad_gpu_params q = *params;
-    q.warps_per_block = wpb;
-    q.priority_permille = pri;
-    q.long_visit = lv;
-    nomad_gpu_tune_trial t{wpb, pri, lv, NOMAD_OK, -1.0};
+    q.warps_per_block = t.warps_per_block;
+    q.priority_permille = t.priority_permille;
+    q.long_visit = t.long_visit;
     nomad_gpu_ctx* c = nullptr;
     t.status = nomad_gpu_init(&c, prob, &q);
     if (t.status == NOMAD_OK) {
@@ -904,45 +901,13 @@ int nomad_gpu_autotune(const nomad_gpu_problem* prob, nomad_gpu_params* params, 
       }
     }
     nomad_gpu_destroy(c);
-    done.push_back(t);
-    return t.status == NOMAD_OK ? t.device_ms : -1.0;
   };
-  auto better = [](double a, double b) { return a >= 0 && (b < 0 || a < b); };
-  // warps per block: the compiled maximum (what 0 resolves to), then fewer
-  int32_t pri = params->priority_permille == 0 ? 50 : params->priority_permille;  // the defaults, spelt out
-  int32_t lv = params->long_visit > 0 ? params->long_visit : 14;
-  double best = run(0, pri, lv);
-  const int32_t cap = done.empty() || done.back().status != NOMAD_OK ? 0 : done.back().warps_per_block;
-  int32_t wpb = cap;
-  for (int32_t w : {cap - 2, cap - 4}) {
-    if (w < 1) continue;
-    const double ms = run(w, pri, lv);
-    if (better(ms, best)) {
-      best = ms;
-      wpb = w;
-    }
-  }
-  for (int32_t p : {25, 50, 100, -1}) {
-    const double ms = run(wpb, p, lv);
-    if (better(ms, best)) {
-      best = ms;
-      pri = p;
-    }
-  }
-  for (int32_t l : {10, 14, 20}) {
-    const double ms = run(wpb, pri, l);
-    if (better(ms, best)) {
-      best = ms;
-      lv = l;
-    }
-  }
+  int32_t wpb = 0, pri = 0, lv = 0;
+  const bool ok = nomad::tune_descent(params->priority_permille, params->long_visit, measure, done, &wpb, &pri, &lv);
   const int32_t stored = std::min<int32_t>(max_trials, static_cast<int32_t>(done.size()));
   for (int32_t i = 0; i < stored; ++i) trials[i] = done[i];
   if (n_trials) *n_trials = stored;
-  if (best < 0) {
-    const int32_t st = done.empty() ? NOMAD_ERR_INVALID_ARG : done.front().status;
-    NOMAD_FAIL(st, "no configuration completed an epoch");
-  }
+  if (!ok) NOMAD_FAIL(done.front().status, "no configuration completed an epoch");
   params->warps_per_block = wpb;
   params->priority_permille = pri;
   params->long_visit = lv;

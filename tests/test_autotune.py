@@ -2,6 +2,10 @@
 (warps per block, priority threshold, long-visit length) by coordinate descent over fresh
 contexts.  Checked: the trials it reports ran, the configuration it returns is the
 fastest of them, training with it updates every rating, and other modes are refused."""
+import os
+import shutil
+import subprocess
+
 import pytest
 
 from test_gpu_parity import LR, DR, REG
@@ -37,3 +41,20 @@ def test_autotune_refuses_other_modes(ng):
     with pytest.raises(ng.NomadError) as e:
         ng.autotune(train, test, epochs=0, dim=16)
     assert e.value.status == -1
+
+
+def test_search_on_synthetic_costs(tmp_path):
+    """The search itself (nomad_gb300/csrc/tune.h), compiled with g++ against synthetic
+    epoch-time models by tests/tune_check.cpp: no GPU."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    exe = str(tmp_path / "tune_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I" + os.path.join(root, "include"),
+                    "-I" + os.path.join(root, "nomad_gb300", "csrc"), "-o", exe,
+                    os.path.join(here, "tune_check.cpp")], check=True, timeout=300)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "tune ok" in r.stdout

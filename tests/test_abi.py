@@ -66,6 +66,25 @@ def test_invalid_arguments_are_statuses(ng):
     assert e.value.status == -1 and "ABI" in str(e.value)
 
 
+@pytest.mark.parametrize("kw,status,words", [
+    (dict(dim=-3), -1, "dim"),
+    (dict(init_parts=0), -1, "init_parts"),
+    (dict(precision=7), -1, "precision"),
+    (dict(lrate=-0.1), -1, "non-negative"),
+    (dict(reg=float("nan")), -1, "non-negative"),
+    (dict(lr_strategy=5), -1, "lr_strategy"),
+    (dict(mode="async", lr_strategy="bold"), -9, "bold driver"),
+])
+def test_parameters_are_checked_before_any_device_work(ng, kw, status, words):
+    """Every parameter check of nomad_gpu_init happens on the host, before the device is
+    touched, and names the field; so these run without a GPU."""
+    train, test = ng.synth(ng.synth_spec(1, m=40, n=30, nnz_train=200, nnz_test=20))
+    with pytest.raises(ng.NomadError) as e:
+        ng.Nomad(train, test, **kw)
+    assert e.value.status == status
+    assert words in str(e.value)
+
+
 def test_no_device_is_a_status(ng):
     if ng.device_ok(0):
         pytest.skip("a GB300 is present")

@@ -231,15 +231,75 @@ int nomad_io_write_factors(const char* path, int32_t m, int32_t n, int32_t dim,
   return NOMAD_OK;
 }
 
+namespace {
+
+// The 64-bit Mersenne Twister with std::mt19937_64's parameters (Matsumoto and
+// Nishimura's MT19937-64), producing 312 tempered outputs per twist, and the values of
+// std::uniform_real_distribution<double>(0, b) drawn from it as C++ specifies them
+// (generate_canonical: one 64-bit draw x gives x / 2^64, or the largest double below 1
+// when that rounds to 1; then times b), narrowed to float.  Identical to drawing through
+// the standard library one value at a time, and faster.
+class Mt64Uniform {
+ public:
+  explicit Mt64Uniform(uint64_t seed) {
+    mt_[0] = seed;
+    for (int i = 1; i < kN; ++i) mt_[i] = 6364136223846793005ULL * (mt_[i - 1] ^ (mt_[i - 1] >> 62)) + static_cast<uint64_t>(i);
+  }
+  void fill(float* dst, int64_t count, double b) {
+    const double below_one = std::nextafter(1.0, 0.0);
+    while (count > 0) {
+      if (pos_ == kN) twist();
+      const int take = static_cast<int>(std::min<int64_t>(count, kN - pos_));
+      for (int k = 0; k < take; ++k) {
+        double c = static_cast<double>(out_[pos_ + k]) * 0x1p-64;
+        if (c >= 1.0) c = below_one;
+        dst[k] = static_cast<float>(c * b + 0.0);
+      }
+      pos_ += take;
+      dst += take;
+      count -= take;
+    }
+  }
+
+ private:
+  static constexpr int kN = 312, kM = 156;
+  void twist() {
+    constexpr uint64_t kUpper = 0xFFFFFFFF80000000ULL, kLower = 0x7FFFFFFFULL, kA = 0xB5026F5AA96619E9ULL;
+    auto step = [&](int i, int next, int far) {
+      const uint64_t x = (mt_[i] & kUpper) | (mt_[next] & kLower);
+      mt_[i] = mt_[far] ^ (x >> 1) ^ ((x & 1) ? kA : 0);
+    };
+    int i = 0;
+    for (; i < kN - kM; ++i) step(i, i + 1, i + kM);
+    for (; i < kN - 1; ++i) step(i, i + 1, i + kM - kN);
+    step(kN - 1, 0, kM - 1);
+    for (int k = 0; k < kN; ++k) {
+      uint64_t y = mt_[k];
+      y ^= (y >> 29) & 0x5555555555555555ULL;
+      y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+      y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+      y ^= y >> 43;
+      out_[k] = y;
+    }
+    pos_ = 0;
+  }
+  uint64_t mt_[kN];
+  uint64_t out_[kN];
+  int pos_ = kN;
+};
+
+}  // namespace
+
 // nb_main.cpp:450-455 (rows of part t from mt19937_64(seed + rank*131 + t + 1)) and
 // nb_main.cpp:71-92 (every column's values from mt19937_64(seed + rank*131 + 139)),
-// single rank.  Row blocks follow read_data's ceil(m / parts) split (nb_data.cpp:83-89).
+// single rank, each value uniform_real_distribution<double>(0, 1/sqrt(dim)) narrowed to
+// float.  Row blocks follow read_data's ceil(m / parts) split (nb_data.cpp:83-89).
 int nomad_reference_init(int32_t m, int32_t n, int32_t dim, uint64_t seed,
                          int32_t init_parts, float* W, float* H) {
   nomad::clear_last_error();
   if (m < 0 || n < 0 || dim <= 0 || init_parts <= 0)
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_reference_init");
-  std::uniform_real_distribution<double> init_dist(0, 1.0 / std::sqrt(dim));
+  const double b = 1.0 / std::sqrt(dim);
   const int32_t P = init_parts;
   const int32_t rows_per_part = m / P + ((m % P > 0) ? 1 : 0);
   if (W) {
@@ -247,16 +307,11 @@ int nomad_reference_init(int32_t m, int32_t n, int32_t dim, uint64_t seed,
       for (int64_t t = lo_t; t < hi_t; ++t) {
         const int64_t lo = std::min<int64_t>(int64_t(rows_per_part) * t, m);
         const int64_t hi = std::min<int64_t>(int64_t(rows_per_part) * (t + 1), m);
-        std::mt19937_64 rng(seed + 0 * 131 + t + 1);
-        std::uniform_real_distribution<double> dist(0, 1.0 / std::sqrt(dim));
-        for (int64_t i = lo * dim; i < hi * dim; ++i) W[i] = static_cast<float>(dist(rng));
+        Mt64Uniform(seed + 0 * 131 + t + 1).fill(W + lo * dim, (hi - lo) * dim, b);
       }
     });
   }
-  if (H) {
-    std::mt19937_64 rng(seed + 0 * 131 + 139);
-    for (int64_t i = 0; i < int64_t(n) * dim; ++i) H[i] = static_cast<float>(init_dist(rng));
-  }
+  if (H) Mt64Uniform(seed + 0 * 131 + 139).fill(H, int64_t(n) * dim, b);
   return NOMAD_OK;
 }
 

@@ -109,8 +109,11 @@ def test_factor_dump_format(ng, tmp_path):
 
 
 def test_reference_init_matches_oracle(ng, O):
+    # small and large parts (the values come 312 to a twist), dim 1 (bound 1.0), more parts
+    # than rows, a seed above 2^63
     for m, n, dim, seed, parts in [(37, 11, 10, 12345, 1), (100, 7, 33, 99, 4),
-                                   (5, 5, 100, 0, 16)]:
+                                   (5, 5, 100, 0, 16), (3000, 700, 100, 12345, 16),
+                                   (480, 17, 1, 5, 7), (1, 2000, 64, 2**63 + 5, 3)]:
         W, H = ng.reference_init(m, n, dim, seed, parts)
         Wd, Hd = O.init_factors(m, n, dim, seed, parts)
         assert np.array_equal(W, Wd.astype(np.float32))

@@ -1,15 +1,17 @@
-// Invariants of the host-side layout (nomad_gb300/csrc/host_layout.cpp) on seeded
+// Invariants of the host-side layouts (nomad_gb300/csrc/host_layout.cpp) on seeded
 // random matrices, on the CPU: the CSC holds every rating once, columns ascending by
 // row, with the row counts of the input; the worker row blocks are contiguous and cover
 // every row; a column's visits cover its ratings exactly once, each visit a run of rows
 // owned by one worker (or one group of `group` workers for a priority column); routes
 // that keep a group's visits consecutive do so; every active token starts in exactly one
-// queue, at a rank below that queue's count.  Prints "layout ok" and exits 0 when all
-// cases hold.
+// queue, at a rank below that queue's count; the DSGD blocks hold every rating exactly
+// once, in the block of its cell.  Prints "layout ok" and exits 0 when all cases hold.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <set>
+#include <tuple>
 #include <vector>
 
 #include "layout.h"
@@ -141,6 +143,48 @@ void run_case(int32_t m, int32_t n, int per_row, int32_t P, int balance, int64_t
   }
 }
 
+// DSGD blocks: innerB row blocks x col_blocks column blocks of ceil(m / innerB) rows and
+// ceil(n / col_blocks) columns; every rating exactly once, in the block of its cell
+// (the order inside a block is the fill's; only membership is checked).
+void run_dsgd_case(int32_t m, int32_t n, int per_row, int32_t innerB, int32_t col_blocks) {
+  std::vector<int32_t> rc(m), cols;
+  std::vector<float> vals;
+  for (int32_t i = 0; i < m; ++i) {
+    std::set<int32_t> cs;
+    const int k = static_cast<int>(next_u32() % (2 * per_row + 1));
+    while (static_cast<int>(cs.size()) < std::min(k, n)) cs.insert(static_cast<int32_t>(next_u32() % n));
+    rc[i] = static_cast<int32_t>(cs.size());
+    for (int32_t c : cs) {
+      cols.push_back(c);
+      vals.push_back(static_cast<float>(next_u32() % 1000) / 7.f);
+    }
+  }
+  const int64_t nnz = static_cast<int64_t>(cols.size());
+  nomad_gpu_matrix A{nnz, rc.data(), nullptr, cols.data(), nullptr, vals.data()};
+  nomad::DsgdLayout D;
+  CHECK(nomad::build_dsgd_layout(A, m, n, innerB, col_blocks, D) == 0);
+  CHECK(D.innerBm == std::max(1, m / innerB + (m % innerB ? 1 : 0)));
+  CHECK(D.innerBn == std::max(1, n / col_blocks + (n % col_blocks ? 1 : 0)));
+  const int64_t nb = static_cast<int64_t>(innerB) * col_blocks;
+  CHECK(D.blk_ptr.size() == static_cast<size_t>(nb) + 1 && D.blk_ptr[0] == 0 && D.blk_ptr[nb] == nnz);
+  std::multiset<std::tuple<int32_t, int32_t, float>> want, got;
+  int64_t o = 0;
+  for (int32_t i = 0; i < m; ++i)
+    for (int32_t q = 0; q < rc[i]; ++q, ++o) want.insert({i, cols[o], vals[o]});
+  for (int64_t b = 0; b < nb; ++b) {
+    CHECK(D.blk_ptr[b] <= D.blk_ptr[b + 1]);
+    for (int64_t e = D.blk_ptr[b]; e < D.blk_ptr[b + 1]; ++e) {
+      const int32_t r = D.rates[4 * e], c = D.rates[4 * e + 1];
+      float v;
+      std::memcpy(&v, &D.rates[4 * e + 2], 4);
+      CHECK(D.rates[4 * e + 3] == 0);
+      CHECK(static_cast<int64_t>(r / D.innerBm) * col_blocks + c / D.innerBn == b);
+      got.insert({r, c, v});
+    }
+  }
+  CHECK(got == want);
+}
+
 }  // namespace
 
 int main() {
@@ -151,6 +195,9 @@ int main() {
   run_case(5000, 300, 20, 40, 1, 100, 10, true, 1);
   run_case(400, 50, 5, 7, 1, 30, 3, true, 2);
   run_case(17, 9, 3, 30, 1, 0, 1, false, 4);  // more workers than rows
+  run_dsgd_case(500, 80, 6, 4, 4);
+  run_dsgd_case(501, 83, 6, 7, 14);  // DSGD++'s innerB x 2 innerB grid, ragged edges
+  run_dsgd_case(3, 2, 1, 8, 8);      // more blocks than rows and columns
   std::printf("%s\n", g_fail ? "layout FAILED" : "layout ok");
   return g_fail ? 1 : 0;
 }

@@ -1,8 +1,8 @@
 """Host-side layout invariants, on the CPU: the CSC build and the route layout of the
 asynchronous kernel (row blocks, visit lists, priority groups, grouped routes, initial
-queues) checked by tests/layout_check.cpp against the definitions, for several worker
-counts, thread counts and both row-block balances, with and without the row counts that
-the CSC build hands to the layout."""
+queues) and the DSGD / DSGD++ blocks, checked by tests/layout_check.cpp against the
+definitions, for several worker counts, thread counts and both row-block balances, with and
+without the row counts that the CSC build hands to the layout."""
 import os
 import shutil
 import subprocess

@@ -248,8 +248,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
         const int32_t i = order[t];
         const nomad::Csc& c = csc_tr[i];
         const nomad::BatchProblem& pb = b->probs[i];
-        std::vector<int64_t> row_nnz(pb.m, 0);
-        for (const auto& r : c.ratings) ++row_nnz[r.row];
+        const std::vector<int32_t>& row_nnz = c.row_nnz;  // ratings per row, from the CSC build
         int32_t* rs = rs_all.data() + pb.rs_off;
         const int64_t nz = c.nnz();
         int64_t acc = 0;

@@ -26,7 +26,8 @@ struct RowMajor {
   float val(int64_t i) const { return v64 ? static_cast<float>(v64[i]) : v32[i]; }
 };
 
-int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R, int threads) {
+int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R, int threads,
+                 bool check_cols = true) {
   if (A.nnz < 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "negative nnz");
   if (A.nnz > 0 && (!A.cols || (!A.vals_f64 && !A.vals_f32)))
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "rating set has nnz > 0 but null arrays");
@@ -62,6 +63,7 @@ int to_row_major(const nomad_gpu_matrix& A, int32_t m, int32_t n, RowMajor& R, i
     R.cols = R.own_cols.data();
     R.v32 = R.own_vals.data();
   }
+  if (!check_cols) return NOMAD_OK;  // the caller checks them in its own pass
   // first out-of-range column index, checked in parallel
   std::atomic<int64_t> bad{A.nnz};
   const int32_t* cols = R.cols;
@@ -106,7 +108,7 @@ float step_size_f32(double lrate, double drate, int32_t cnt) {
 
 int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int threads) {
   RowMajor R;
-  int rc = to_row_major(A, m, n, R, threads);
+  int rc = to_row_major(A, m, n, R, threads, false);
   if (rc) return rc;
   const int64_t nnz = A.nnz;
   out.m = m;
@@ -122,10 +124,20 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
   // column histogram per chunk, then each chunk scatters in order.
   const int T = std::max<int>(1, std::min<int64_t>(threads, std::max<int64_t>(1, nnz / 65536)));
   std::vector<std::vector<int64_t>> hist(T, std::vector<int64_t>(n, 0));
+  std::vector<int64_t> first_bad(T, nnz);  // the column indices are checked in the same pass
   parallel_chunks(nnz, T, [&](int t, int64_t lo, int64_t hi) {
     std::vector<int64_t>& h = hist[t];
-    for (int64_t i = lo; i < hi; ++i) h[R.cols[i]]++;
+    for (int64_t i = lo; i < hi; ++i) {
+      const int32_t c = R.cols[i];
+      if (static_cast<uint32_t>(c) >= static_cast<uint32_t>(n)) {
+        first_bad[t] = i;
+        break;
+      }
+      h[c]++;
+    }
   });
+  const int64_t bad = *std::min_element(first_bad.begin(), first_bad.end());
+  if (bad < nnz) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "column index %d out of range [0, %d)", R.cols[bad], n);
   for (int32_t j = 0; j < n; ++j) {
     int64_t s = 0;
     for (int t = 0; t < T; ++t) s += hist[t][j];

@@ -185,6 +185,24 @@ void run_dsgd_case(int32_t m, int32_t n, int per_row, int32_t innerB, int32_t co
   CHECK(got == want);
 }
 
+// Out-of-range column indices anywhere in the input (first, middle, last entry; too large
+// or negative) are an invalid argument, for one and several threads.
+void run_bad_column_cases() {
+  const int32_t m = 3000, n = 40;
+  for (int threads : {1, 4})
+    for (int64_t where : {int64_t(0), int64_t(60000), int64_t(m) * n - 1})
+      for (int32_t badc : {n, -1}) {
+        std::vector<int32_t> rc(m, n), cols;
+        for (int32_t i = 0; i < m; ++i)
+          for (int32_t j = 0; j < n; ++j) cols.push_back(j);
+        cols[static_cast<size_t>(where)] = badc;
+        std::vector<float> vals(cols.size(), 1.f);
+        nomad_gpu_matrix A{static_cast<int64_t>(cols.size()), rc.data(), nullptr, cols.data(), nullptr, vals.data()};
+        nomad::Csc csc;
+        CHECK(nomad::build_csc(A, m, n, csc, threads) == NOMAD_ERR_INVALID_ARG);
+      }
+}
+
 }  // namespace
 
 int main() {
@@ -195,6 +213,7 @@ int main() {
   run_case(5000, 300, 20, 40, 1, 100, 10, true, 1);
   run_case(400, 50, 5, 7, 1, 30, 3, true, 2);
   run_case(17, 9, 3, 30, 1, 0, 1, false, 4);  // more workers than rows
+  run_bad_column_cases();
   run_dsgd_case(500, 80, 6, 4, 4);
   run_dsgd_case(501, 83, 6, 7, 14);  // DSGD++'s innerB x 2 innerB grid, ragged edges
   run_dsgd_case(3, 2, 1, 8, 8);      // more blocks than rows and columns

@@ -40,6 +40,9 @@ def test_mode_options_are_validated(ng):
     assert r.returncode == 1 and "--lr_strategy bold needs --mode dsgd or dsgdpp." in r.stderr
     assert run("--path", "x", "--mode", "sgd").returncode == 1
     assert "dsgdpp" in run("--help").stderr
+    r = run("--path", "x", "--autotune", "many")
+    assert r.returncode == 1 and "'--autotune' is invalid" in r.stderr
+    assert "--autotune" in run("--help").stderr
 
 
 def test_checkpoint_options_are_validated(ng):

@@ -17,6 +17,7 @@
 #include <fstream>
 #include <mutex>
 #include <numeric>
+#include <queue>
 #include <random>
 #include <thread>
 #include <vector>
@@ -253,6 +254,136 @@ int async_run(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr,
   if (updates) *updates = std::accumulate(num_updates.begin(), num_updates.end(), int64_t(0));
   if (failures) *failures = std::accumulate(num_failures.begin(), num_failures.end(), int64_t(0));
   if (train_seconds) *train_seconds = std::chrono::duration<double>(t1 - t0).count();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Asynchronous NOMAD with P workers under a deterministic timing model.
+//
+// The reference with --nthreads P (one rank) is nondeterministic: which token a worker
+// pops depends on thread timing.  This restatement runs the same algorithm on one host
+// thread as a discrete-event simulation, so that a P-worker trajectory can be computed
+// exactly and repeatably:
+//  * rows: P contiguous parts, either ceil(m/P) rows each (read_data,
+//    nb_data.cpp:83-89) or parts of about nnz/P ratings each;
+//  * routes: each column's permutation of the P workers drawn as nb_main.cpp:79-96 does
+//    (one mt19937_64(seed + 137), set_perm = identity + std::shuffle, pool.cpp:32-38, in
+//    column order); a visit to a worker without ratings of the column changes nothing
+//    (nb_main.cpp:520 runs zero iterations), so the route keeps only the other workers;
+//  * step: every worker sees a column once per pass, so its per-worker count
+//    col_update_counts (nb_main.cpp:458-459, 544) equals the pass number;
+//  * time: a visit of len ratings occupies its worker for visit_cost + rating_cost*len,
+//    a token reaches its next worker hop_cost after the visit ends, a worker takes its
+//    queue in FIFO order (tbb::concurrent_queue) and ties are broken by event order.
+// Each epoch every token starts at its route's first worker, queues filled in column
+// order.  The per-visit arithmetic is visit_column (nb_main.cpp:520-542) over the
+// worker's run of the column (rows ascending, a contiguous run of the CSC).
+// ---------------------------------------------------------------------------------
+template <typename S>
+int async_sim(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr, const int32_t* row_idx,
+              const double* vals, S* W, S* H, int32_t P, int32_t partition, int32_t first_epoch,
+              int32_t n_epochs, double lrate, double drate, double reg, uint64_t seed, double visit_cost,
+              double rating_cost, double hop_cost, double* epoch_err) {
+  if (P <= 0 || dim <= 0 || m < 0 || n < 0 || n_epochs < 0 || first_epoch < 0) return -1;
+  const int64_t nnz = n > 0 ? col_ptr[n] : 0;
+  // row parts: part_lo[p] .. part_lo[p + 1]
+  std::vector<int32_t> part_lo(P + 1, m);
+  if (partition == 0) {
+    const int64_t rpp = m / P + ((m % P > 0) ? 1 : 0);
+    for (int32_t p = 0; p <= P; ++p) part_lo[p] = static_cast<int32_t>(std::min<int64_t>(rpp * p, m));
+  } else {
+    std::vector<int64_t> cnt(static_cast<size_t>(m) + 1, 0);
+    for (int64_t o = 0; o < nnz; ++o) cnt[row_idx[o] + 1]++;
+    for (int32_t r = 0; r < m; ++r) cnt[r + 1] += cnt[r];
+    int32_t r = 0;
+    for (int32_t p = 0; p < P; ++p) {
+      const int64_t goal = (nnz * p + P - 1) / P;
+      while (r < m && cnt[r] < goal) ++r;
+      part_lo[p] = r;
+    }
+    part_lo[P] = m;
+  }
+  std::vector<int32_t> row_part(m);
+  for (int32_t p = 0; p < P; ++p)
+    for (int32_t r = part_lo[p]; r < part_lo[p + 1]; ++r) row_part[r] = p;
+  // each column's visits {worker, start, len} in permutation order
+  struct Visit {
+    int32_t worker;
+    int32_t len;
+    int64_t start;
+  };
+  std::vector<int64_t> vptr(static_cast<size_t>(n) + 1, 0);
+  std::vector<Visit> visits;
+  std::vector<int32_t> perm(P), inv(P);
+  std::mt19937_64 rng_temp(seed + 0 + 137);
+  for (int32_t j = 0; j < n; ++j) {
+    for (int32_t i = 0; i < P; ++i) perm[i] = i;
+    std::shuffle(perm.begin(), perm.end(), rng_temp);
+    for (int32_t i = 0; i < P; ++i) inv[perm[i]] = i;
+    const size_t first = visits.size();
+    for (int64_t o = col_ptr[j]; o < col_ptr[j + 1];) {
+      const int32_t w = row_part[row_idx[o]];
+      int64_t e = o + 1;
+      while (e < col_ptr[j + 1] && row_part[row_idx[e]] == w) ++e;
+      visits.push_back({w, static_cast<int32_t>(e - o), o});
+      o = e;
+    }
+    std::sort(visits.begin() + first, visits.end(),
+              [&](const Visit& a, const Visit& b) { return inv[a.worker] < inv[b.worker]; });
+    vptr[j + 1] = static_cast<int64_t>(visits.size());
+  }
+  std::vector<S> sv;
+  const S* v = nullptr;
+  if (sizeof(S) == sizeof(double)) {
+    v = reinterpret_cast<const S*>(vals);
+  } else {
+    sv = cast_vals<S>(vals, nnz);
+    v = sv.data();
+  }
+  const S lambda = static_cast<S>(reg);
+  struct Event {
+    double t;
+    int64_t seq;
+    int32_t kind;  // 0: a worker's visit ends, 1: a token arrives
+    int32_t a;     // worker (kind 0) or token (kind 1)
+    int32_t b;     // target worker (kind 1)
+    bool operator>(const Event& o) const { return t != o.t ? t > o.t : seq > o.seq; }
+  };
+  for (int32_t ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
+    const S step = step_size<S>(lrate, drate, ep);
+    std::vector<std::deque<int32_t>> q(P);
+    std::vector<int32_t> cur(P, -1), pos(n, 0);
+    std::priority_queue<Event, std::vector<Event>, std::greater<Event>> heap;
+    int64_t seq = 0;
+    double err = 0.0;
+    auto start = [&](int32_t w, double t) {
+      const int32_t j = q[w].front();
+      q[w].pop_front();
+      cur[w] = j;
+      const Visit& vi = visits[vptr[j] + pos[j]];
+      visit_column<S>(H + static_cast<int64_t>(dim) * j, W, dim, row_idx, v, vi.start, vi.start + vi.len, step,
+                      lambda, &err);
+      heap.push({t + visit_cost + rating_cost * vi.len, seq++, 0, w, 0});
+    };
+    for (int32_t j = 0; j < n; ++j)
+      if (vptr[j + 1] > vptr[j]) q[visits[vptr[j]].worker].push_back(j);
+    for (int32_t w = 0; w < P; ++w)
+      if (!q[w].empty()) start(w, 0.0);
+    while (!heap.empty()) {
+      const Event e = heap.top();
+      heap.pop();
+      if (e.kind == 0) {
+        const int32_t w = e.a, j = cur[w];
+        cur[w] = -1;
+        if (++pos[j] < vptr[j + 1] - vptr[j]) heap.push({e.t + hop_cost, seq++, 1, j, visits[vptr[j] + pos[j]].worker});
+        if (!q[w].empty()) start(w, e.t);
+      } else {
+        q[e.b].push_back(e.a);
+        if (cur[e.b] < 0) start(e.b, e.t);
+      }
+    }
+    if (epoch_err) epoch_err[ep - first_epoch] = err;
+  }
   return 0;
 }
 
@@ -555,6 +686,21 @@ int oracle_async_f64(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr,
   return async_run<double>(m, n, dim, col_ptr, row_idx, vals, W, H, nthreads,
                            n_epochs, timeout_sec, lrate, drate, reg, seed, updates,
                            failures, train_seconds);
+}
+
+int oracle_async_sim_f32(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr, const int32_t* row_idx,
+                         const double* vals, float* W, float* H, int32_t P, int32_t partition, int32_t first_epoch,
+                         int32_t n_epochs, double lrate, double drate, double reg, uint64_t seed,
+                         double visit_cost, double rating_cost, double hop_cost, double* epoch_err) {
+  return async_sim<float>(m, n, dim, col_ptr, row_idx, vals, W, H, P, partition, first_epoch, n_epochs, lrate,
+                          drate, reg, seed, visit_cost, rating_cost, hop_cost, epoch_err);
+}
+int oracle_async_sim_f64(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr, const int32_t* row_idx,
+                         const double* vals, double* W, double* H, int32_t P, int32_t partition, int32_t first_epoch,
+                         int32_t n_epochs, double lrate, double drate, double reg, uint64_t seed,
+                         double visit_cost, double rating_cost, double hop_cost, double* epoch_err) {
+  return async_sim<double>(m, n, dim, col_ptr, row_idx, vals, W, H, P, partition, first_epoch, n_epochs, lrate,
+                           drate, reg, seed, visit_cost, rating_cost, hop_cost, epoch_err);
 }
 
 int oracle_dsgd_f32(int32_t m, int32_t n, int32_t dim, int64_t nnz,

@@ -19,10 +19,15 @@
  *   - DSGD++, bold driver     Code/competitor/dsgdpp.cpp:300-540, :42-69 (blocks);
  *                             sgd-mpi-omp.cpp:122-160 (calobj_mpi), :384-394
  *
- * Parity status: the reference ships no tests, fixtures or golden vectors and cannot
- * be built here (MPI/TBB/Boost/glog absent), so this restatement is pinned only by
- * the C++ standard's own known answer for std::mt19937_64 and by hand-computed
- * known-answer updates (tests/test_oracle.py).  Parity unpinned by the reference.
+ * Parity status: pinned to the reference itself.  The reference ships no tests or
+ * golden vectors, but its updater (Code/nomad/nb_main.cpp, nb_data.cpp, pool.cpp)
+ * compiles unmodified against single-process stand-ins for TBB, glog, boost::format
+ * and MPI (oracle/Makefile.ref, oracle/refshim/), and run on one rank with one thread
+ * it gives the same columns and evaluation sums as oracle_replay_f64 / oracle_sse_f64
+ * bit for bit (tests/test_reference_pin.py, golden outputs in
+ * tests/golden/reference_replay.npz).  The float forms follow the legacy float body,
+ * which cannot be built (it includes a header missing from the reference tree); they
+ * are pinned by the pure-Python restatements of tests/golden/make_golden.py.
  *
  * Data layout conventions used by every entry point:
  *   CSC-by-column: col_ptr[n+1] (int64), row_idx[nnz] (int32, ascending inside a
@@ -100,6 +105,29 @@ int oracle_async_f64(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr,
                      double timeout_sec, double lrate, double drate, double reg,
                      uint64_t seed, int64_t* updates, int64_t* failures,
                      double* train_seconds);
+
+/* Asynchronous NOMAD with P workers as a deterministic discrete-event simulation on one
+ * host thread (the reference with --nthreads P, nb_main.cpp:415-572, whose schedule
+ * depends on thread timing).  Rows in P contiguous parts (partition 0: ceil(m/P) rows,
+ * nb_data.cpp:83-89; partition 1: about nnz/P ratings each); each column's route is its
+ * permutation of the workers drawn with mt19937_64(seed + 137) in column order
+ * (nb_main.cpp:79-96, pool.cpp:32-38) without the workers that hold none of its
+ * ratings; step of pass e = step(cnt = e).  A visit of len ratings takes
+ * visit_cost + rating_cost*len time units, a hop hop_cost; queues are FIFO.  Runs
+ * passes [first_epoch, first_epoch + n_epochs), every token starting each pass at its
+ * route's first worker; epoch_err[i] = the pass's online squared-error sum. */
+int oracle_async_sim_f32(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr,
+                         const int32_t* row_idx, const double* vals, float* W, float* H,
+                         int32_t P, int32_t partition, int32_t first_epoch, int32_t n_epochs,
+                         double lrate, double drate, double reg, uint64_t seed,
+                         double visit_cost, double rating_cost, double hop_cost,
+                         double* epoch_err);
+int oracle_async_sim_f64(int32_t m, int32_t n, int32_t dim, const int64_t* col_ptr,
+                         const int32_t* row_idx, const double* vals, double* W, double* H,
+                         int32_t P, int32_t partition, int32_t first_epoch, int32_t n_epochs,
+                         double lrate, double drate, double reg, uint64_t seed,
+                         double visit_cost, double rating_cost, double hop_cost,
+                         double* epoch_err);
 
 /* DSGD, single process (numprocs = 1 => B = 1, innerB = 2*nthreads), FIXED learning
  * rate schedule lr = 1.5*lrate/(1+decay*iter^1.5).  Input is the row-major file

@@ -233,3 +233,92 @@ def read_matrix(path):
     _check(lib().oracle_read_matrix(bpath, _p(rc), _p(cols), _p(vals)), "read_matrix")
     return {"file_id": int(fid[0]), "m": int(m[0]), "n": int(n[0]),
             "row_counts": rc, "cols": cols, "vals": vals}
+
+
+# ---- the reference's own updater, compiled from the reference tree -------------------
+_REF_LIB_PATH = os.path.join(_HERE, "_ref", "libnomad_ref.so")
+_ref_lib = None
+
+
+def reference_tree():
+    """Path of the reference tree when it is present on this machine, else None."""
+    d = os.environ.get("NOMAD_REFERENCE_DIR", "/root/reference")
+    return d if os.path.isfile(os.path.join(d, "Code", "nomad", "nb_main.cpp")) else None
+
+
+def build_ref():
+    """Compile the reference's updater (oracle/Makefile.ref) when the reference tree is
+    present; returns False when it is not (the GPU machine has no reference tree)."""
+    d = reference_tree()
+    if d is None:
+        return False
+    subprocess.run(["make", "-s", "-C", _HERE, "-f", "Makefile.ref", "REF_DIR=" + d], check=True)
+    return True
+
+
+def ref_lib():
+    global _ref_lib
+    if _ref_lib is None:
+        if not os.path.exists(_REF_LIB_PATH) and not build_ref():
+            raise FileNotFoundError("the reference build oracle/_ref/libnomad_ref.so is absent "
+                                    "and the reference tree is not on this machine")
+        L = ctypes.CDLL(_REF_LIB_PATH)
+        L.ref_replay_f64.restype = ctypes.c_int
+        L.ref_replay_f64.argtypes = [ctypes.c_char_p, _i32, _dbl, _dbl, _dbl, _u64, _i32,
+                                     ctypes.c_char_p, _ptr, _ptr, _ptr, _ptr, _ptr, _ptr, _ptr]
+        _ref_lib = L
+    return _ref_lib
+
+
+def ref_replay(data_dir, n, dim, lrate, drate, reg, seed, epochs, rows_prefix=None):
+    """The reference's updater thread (nb_main.cpp:415-710, one rank, one thread) run for
+    `epochs` passes on <data_dir>/train.dat from the reference init, then its evaluation
+    pass on train.dat and test.dat.  Returns H (n x dim, double), each column's online
+    error, the training/test squared-error sums and counts, and the update count."""
+    H = np.zeros((n, dim), np.float64)
+    col_err = np.zeros(n, np.float64)
+    s = np.zeros(2, np.float64)
+    c = np.zeros(3, np.int64)
+    rc = ref_lib().ref_replay_f64(os.fsencode(data_dir), dim, lrate, drate, reg, seed, epochs,
+                                  os.fsencode(rows_prefix) if rows_prefix else None,
+                                  _p(H), _p(col_err), s[0:].ctypes.data, c[0:].ctypes.data,
+                                  s[1:].ctypes.data, c[1:].ctypes.data, c[2:].ctypes.data)
+    _check(rc, "ref_replay_f64")
+    return {"H": H, "col_err": col_err, "train_sse": float(s[0]), "train_count": int(c[0]),
+            "test_sse": float(s[1]), "test_count": int(c[1]), "updates": int(c[2])}
+
+
+def write_matrix(path, m, n, row_counts, cols, vals, file_id=1211216):
+    """train.dat/test.dat writer for the checks (the format nb_data.cpp:19-176 reads:
+    id, m, n, nnz (int32, or int64 under id 1015), row counts, column indices, values)."""
+    row_counts = np.ascontiguousarray(row_counts, np.int32)
+    cols = np.ascontiguousarray(cols, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    with open(path, "wb") as f:
+        if file_id == 1015:
+            np.array([file_id, m, n], np.int32).tofile(f)
+            np.array([cols.size], np.int64).tofile(f)
+        else:
+            np.array([file_id, m, n, cols.size], np.int32).tofile(f)
+        row_counts.tofile(f)
+        cols.tofile(f)
+        vals.tofile(f)
+
+
+def async_sim(csc, W, H, P, first_epoch, n_epochs, lrate, drate, reg, seed=12345, partition=1,
+              visit_cost=3000.0, rating_cost=400.0, hop_cost=3000.0):
+    """P-worker asynchronous NOMAD as a deterministic event simulation (in place on W, H;
+    float32 or float64); returns each pass's online squared-error sum."""
+    col_ptr, row_idx, vals = csc
+    m, dim = W.shape
+    n = H.shape[0]
+    assert W.flags.c_contiguous and H.flags.c_contiguous and W.dtype == H.dtype
+    err = np.zeros(max(n_epochs, 1), np.float64)
+    L = lib()
+    f = L.oracle_async_sim_f32 if W.dtype == np.float32 else L.oracle_async_sim_f64
+    f.restype = ctypes.c_int
+    f.argtypes = [_i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _ptr, _i32, _i32, _i32, _i32,
+                  _dbl, _dbl, _dbl, _u64, _dbl, _dbl, _dbl, _ptr]
+    _check(f(m, n, dim, _p(col_ptr), _p(row_idx), _p(vals), _p(W), _p(H), P, partition, first_epoch,
+             n_epochs, lrate, drate, reg, seed, visit_cost, rating_cost, hop_cost, _p(err)), "async_sim")
+    return err[:n_epochs]

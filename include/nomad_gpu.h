@@ -276,13 +276,22 @@ int nomad_gpu_autotune(const nomad_gpu_problem* prob, nomad_gpu_params* params, 
  *            (precision NOMAD_PREC_FP32, kpad = dim rounded up to 4) or bf16
  *            (NOMAD_PREC_BF16_SR, kpad = dim rounded up to 8); padding zero;
  *   ratings  nnz pairs {int32 row, float value}, grouped by column;
- *   col_ptr  n + 1 int64 offsets of the columns in `ratings`.
+ *   col_ptr  n + 1 int64 offsets of the columns in `ratings`: col_ptr[0] == 0,
+ *            non-decreasing, col_ptr[n] == nnz (not checked: the host cannot read
+ *            them; an offset table that breaks this reads past `ratings`).
+ * W and H must be 16-byte aligned, ratings, col_ptr and sse_out 8-byte aligned (a
+ * sub-view at an odd offset is refused with NOMAD_ERR_INVALID_ARG before any device
+ * work), and nnz > 0 needs n > 0.  nnz = 0 writes 0 to *sse_out.
  * blocks = 0 picks 8 per SM (at most NOMAD_NOALLOC_MAX_BLOCKS); larger values are
  * rejected with NOMAD_ERR_INVALID_ARG.  The first call on a device looks up the
- * array's device address with that device made current (it is restored afterwards);
- * make that first call before capturing any stream.  Every call uses the same array,
- * so calls that overlap on the GPU (different streams, no ordering) race and give
- * wrong sums; each call rewrites every partial it reads, so nothing needs clearing. */
+ * array's device address with that device made current (it is restored afterwards)
+ * and keeps it for the life of the process, so a device reset (cudaDeviceReset, or
+ * re-creating the primary context) after that first call is not supported; make that
+ * first call before capturing any stream.  Every call uses the same array, so calls
+ * that overlap on the GPU (different streams, no ordering) race and give wrong sums;
+ * each call rewrites every partial it reads, so nothing needs clearing.  Work is
+ * ordered on `stream` only: inputs produced by earlier work on the same stream are
+ * read after it. */
 #define NOMAD_NOALLOC_MAX_BLOCKS 2048
 int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t n, int32_t dim,
                           const void* W, const void* H, const void* ratings,

@@ -346,6 +346,15 @@ extern "C" int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t 
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "unknown precision %d", precision);
   if (n < 0 || dim <= 0 || nnz < 0 || !sse_out || (nnz > 0 && (!W || !H || !ratings || !col_ptr)))
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid sizes or null pointers");
+  if (n == 0 && nnz > 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "nnz = %lld ratings but no column", (long long)nnz);
+  // The kernel reads rows as 16-byte vectors and ratings / offsets as 8-byte words: a
+  // misaligned pointer (a view at an odd offset) would fault and poison the caller's
+  // context, so it is refused here, before any device work.
+  auto misaligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) != 0; };
+  if (misaligned(W, 16) || misaligned(H, 16))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "W and H must be 16-byte aligned");
+  if (misaligned(ratings, 8) || misaligned(col_ptr, 8) || misaligned(sse_out, 8))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "ratings, col_ptr and sse_out must be 8-byte aligned");
   if (blocks < 0 || blocks > NOMAD_NOALLOC_MAX_BLOCKS)
     NOMAD_FAIL(NOMAD_ERR_INVALID_ARG,
                "blocks = %d exceeds the fixed partial-sum array of %d blocks", blocks,

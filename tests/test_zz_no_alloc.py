@@ -93,3 +93,63 @@ def test_noalloc_rejects_too_many_blocks(ng, gpu_ok):
     torch.cuda.synchronize()
     ref = float(np.sum(train.vals.astype(np.float32).astype(np.float64) ** 2))
     assert abs(out.item() - ref) <= TOL * ref
+
+
+def test_noalloc_refuses_misaligned_and_columnless_input(ng, gpu_ok):
+    """A view at an odd offset is refused on the host (no kernel runs), and so are
+    ratings without any column."""
+    torch = pytest.importorskip("torch")
+    train, _ = _problem(ng)
+    dim = 8
+    W = np.zeros((train.m, dim), np.float32)
+    H = np.zeros((train.n, dim), np.float32)
+    Wd, Hd, pairs, col_ptr = _device_layout(torch, ng, train, W, H, "fp32")
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    L = ng.lib()
+    E = ng._abi.ERR_INVALID_ARG
+    args = [0, 0, train.n, dim, Wd.data_ptr(), Hd.data_ptr(), pairs.data_ptr(), col_ptr.data_ptr(),
+            train.nnz, 0, out.data_ptr(), None]
+    for i, off in ((4, 4), (5, 8), (6, 4), (7, 4), (10, 4)):
+        bad = list(args)
+        bad[i] += off
+        assert L.nomad_gpu_sse_noalloc(*bad) == E, i
+        assert b"aligned" in L.nomad_gpu_last_error()
+    bad = list(args)
+    bad[2] = 0
+    assert L.nomad_gpu_sse_noalloc(*bad) == E
+    torch.cuda.synchronize()
+    assert out.abs().sum().item() == 0.0
+
+
+def test_noalloc_empty_set_and_side_stream(ng, gpu_ok):
+    """nnz = 0 writes 0; on a side stream, a call ordered after the kernels that fill
+    its inputs on that same stream reads the filled inputs."""
+    torch = pytest.importorskip("torch")
+    train, test = _problem(ng)
+    dim = 64
+    rng = np.random.default_rng(8)
+    W = (rng.standard_normal((train.m, dim)) * 0.1).astype(np.float32)
+    H = (rng.standard_normal((train.n, dim)) * 0.1).astype(np.float32)
+    with ng.Nomad(train, test, W0=W, H0=H, dim=dim, precision="fp32") as nm:
+        ref, _, _, _ = nm.sse()
+    L = ng.lib()
+    Wd, Hd, pairs, col_ptr = _device_layout(torch, ng, train, W, H, "fp32")
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    rc = L.nomad_gpu_sse_noalloc(0, 0, train.n, dim, Wd.data_ptr(), Hd.data_ptr(), pairs.data_ptr(),
+                                 col_ptr.data_ptr(), 0, 0, out.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert out.item() == 0.0
+    side = torch.cuda.Stream()
+    W2 = torch.empty_like(Wd)
+    H2 = torch.empty_like(Hd)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        W2.copy_(Wd)  # producers of the inputs, on the side stream
+        H2.copy_(Hd)
+        rc = L.nomad_gpu_sse_noalloc(0, 0, train.n, dim, W2.data_ptr(), H2.data_ptr(), pairs.data_ptr(),
+                                     col_ptr.data_ptr(), train.nnz, 0, out.data_ptr(),
+                                     ctypes.c_void_p(side.cuda_stream))
+        assert rc == 0, L.nomad_gpu_last_error()
+    side.synchronize()
+    assert abs(out.item() - ref) <= TOL * ref, (out.item(), ref)

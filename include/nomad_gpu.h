@@ -95,7 +95,9 @@ typedef struct nomad_gpu_params {
                           REPLAY always uses it                                      */
   int32_t spin_budget_ms; /* device waits give up after this long without global
                              progress and the call returns NOMAD_ERR_TIMEOUT (2000)  */
-  int32_t debug_flags; /* test hooks; bit 0 = enqueue no tokens (forces a timeout)   */
+  int32_t debug_flags; /* test hooks; bit 0 = enqueue no tokens (forces a timeout);   *
+                        * bit 1 = one worker per thread block never joins a block     *
+                        * visit (the others' join wait runs out: a timeout)           */
   int32_t long_visit;  /* ASYNC: visits with at least this many ratings run the blocked
                           (7-rating) path with TMA-staged rows; 0 = default 14        */
   int32_t priority_permille; /* ASYNC: columns with at least this many permille of the

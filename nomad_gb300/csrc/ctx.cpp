@@ -461,6 +461,7 @@ int epoch_async(nomad_gpu_ctx* c, int32_t E, nomad_gpu_epoch_stats* st) {
   a.exact = c->prm.exact;
   a.warps_per_block = c->wpb;
   a.grid = c->grid;
+  a.debug_flags = c->prm.debug_flags;
   // Seeding reads the ring geometry (a.P) and must follow every assignment above; it is
   // part of the timed epoch.
   CK(cudaEventRecord(c->ev0, c->stream));

@@ -488,9 +488,44 @@ __device__ __forceinline__ CtaRegion cta_region(char* base, int kpad, int esz) {
   return C;
 }
 
+// Non-blocking test of phase `parity` of mbarrier `bar` (acquire, cta scope).
+__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Polls phase `parity` of `bar` until it completes (true) or the launch's budget runs
+// out (false).  The clock is read only after 1,024 unsuccessful polls, and then every
+// 1,024, so a short wait costs no %globaltimer read; the budget counts from the first.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, const nomad::AsyncArgs& a) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_test_wait(bar, parity)) return true;
+    if ((it & 1023u) == 0) {
+      const uint64_t now = nd::globaltimer();
+      if (t0 == 0) t0 = now;
+      else if (static_cast<int64_t>(now - t0) > a.budget_ns) return false;
+    }
+  }
+}
+
+// Barrier of the block's live compute warps between the phases of a block visit (named
+// barrier 1 over their nthreads threads).  It cannot wait forever: every live compute
+// warp enters a visit or none does (cta_join), and a visit has no early exit and no
+// wait on another agent -- its only other waits are cp.async.wait_group on its own
+// copies -- so every warp reaches every barrier after a bounded amount of work.  (An
+// mbarrier-based barrier in its place measured about twice the epoch time.)
 __device__ __forceinline__ void bar_sync_named(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
+
 __device__ __forceinline__ int ld_volatile_shared(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
 __device__ __forceinline__ void st_volatile_shared(int* p, int v) { *reinterpret_cast<volatile int*>(p) = v; }
 
@@ -515,34 +550,38 @@ __device__ __forceinline__ void mma_bf16_k8(float (&d)[4], uint32_t a0, uint32_t
       : "r"(a0), "r"(a1), "r"(b0));
 }
 
+// x = hi + lo with hi the TF32 rounding of x and lo the TF32 rounding of the rest: the
+// split of the 3xTF32 scheme (products hi*hi + hi*lo + lo*hi, the lo*lo term dropped),
+// which keeps about fp32 accuracy on the TF32 tensor-core path.
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_bits(x);
+  lo = tf32_bits(x - __uint_as_float(hi));
+}
+
 // One 16x8 tile of G = X X^T: rows r0.., columns n0.. (fragment layouts of mma.m16n8k8 /
-// m16n8k16: g = lane / 4 selects the row, t = lane % 4 the k pair or k element).  G only
-// enters the chain multiplied by eta e_t, so TF32 operands (10-bit mantissa) move e_t by
-// ~1e-3 * eta |e| |G| per step -- far below fp32 noise in w; b = X h stays in fp32.
+// m16n8k16: g = lane / 4 selects the row, t = lane % 4 the k pair or k element).  fp32
+// rows: 3xTF32, three mma per k step (hi*hi into one accumulator, hi*lo + lo*hi into
+// another, summed at the end), so G carries close to fp32 precision like the rest of
+// the fp32 form; b = X h is computed separately in fp32.
 __device__ __forceinline__ void gram_tile(const float* X, int sw, int kpad, int r0, int n0, float (&d)[4], int lane) {
   const int g = lane >> 2, t = lane & 3;
   const float* A0 = X + (r0 + g) * sw;
   const float* A1 = A0 + 8 * sw;
   const float* B = X + (n0 + g) * sw;
-  float d2[4] = {0.f, 0.f, 0.f, 0.f};  // second accumulator: two independent mma chains
+  float d2[4] = {0.f, 0.f, 0.f, 0.f};  // the cross terms hi*lo + lo*hi
   const int kmma = (kpad + 7) / 8 * 8;  // the row padded with zeros to whole k8 steps
-  int k0 = 0;
 #pragma unroll 2
-  for (; k0 + 16 <= kmma; k0 += 16) {
-    const uint32_t a[4] = {tf32_bits(A0[k0 + t]), tf32_bits(A1[k0 + t]), tf32_bits(A0[k0 + t + 4]),
-                           tf32_bits(A1[k0 + t + 4])};
-    const uint32_t b[2] = {tf32_bits(B[k0 + t]), tf32_bits(B[k0 + t + 4])};
-    const uint32_t a2[4] = {tf32_bits(A0[k0 + 8 + t]), tf32_bits(A1[k0 + 8 + t]), tf32_bits(A0[k0 + 12 + t]),
-                            tf32_bits(A1[k0 + 12 + t])};
-    const uint32_t b2[2] = {tf32_bits(B[k0 + 8 + t]), tf32_bits(B[k0 + 12 + t])};
-    mma_tf32(d, a, b);
-    mma_tf32(d2, a2, b2);
-  }
-  if (k0 < kpad) {
-    const uint32_t a[4] = {tf32_bits(A0[k0 + t]), tf32_bits(A1[k0 + t]), tf32_bits(A0[k0 + t + 4]),
-                           tf32_bits(A1[k0 + t + 4])};
-    const uint32_t b[2] = {tf32_bits(B[k0 + t]), tf32_bits(B[k0 + t + 4])};
-    mma_tf32(d, a, b);
+  for (int k0 = 0; k0 < kmma; k0 += 8) {
+    uint32_t ah[4], al[4], bh[2], bl[2];
+    split_tf32(A0[k0 + t], ah[0], al[0]);
+    split_tf32(A1[k0 + t], ah[1], al[1]);
+    split_tf32(A0[k0 + t + 4], ah[2], al[2]);
+    split_tf32(A1[k0 + t + 4], ah[3], al[3]);
+    split_tf32(B[k0 + t], bh[0], bl[0]);
+    split_tf32(B[k0 + t + 4], bh[1], bl[1]);
+    mma_tf32(d2, ah, bl);
+    mma_tf32(d2, al, bh);
+    mma_tf32(d, ah, bh);
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) d[i] += d2[i];
@@ -718,24 +757,23 @@ __device__ __forceinline__ void cta_rows(const char* X, int sw, const int2* rvb,
   }
 }
 
-// Join of the block's live warps before a block visit; false (and the timeout status)
-// when some warp did not arrive within the budget.
+// Join of the block's live warps before a block visit: all of them enter the visit or
+// none does.  A warp whose wait runs out blocks the join's current phase with a pending
+// transaction byte (mbarrier.expect_tx), so a warp arriving later cannot complete it;
+// if the phase had completed just before (the block then lands on the next phase), every
+// warp is in, so the warp undoes the byte (complete_tx) and enters too.  Both operations
+// are atomic on the barrier, so exactly one of the two outcomes holds for every warp.
 __device__ __forceinline__ bool cta_join(uint32_t bar, uint32_t& phase, const nomad::AsyncArgs& a, int lane) {
   int ok = 1;
   if (lane == 0) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-    uint64_t t0 = 0;
-    for (uint32_t it = 0;; ++it) {
-      if (mbar_try_wait(bar, phase)) break;
-      if ((it & 63u) == 0) {
-        const uint64_t now = nd::globaltimer();
-        if (it == 0) {
-          t0 = now;
-        } else if (static_cast<int64_t>(now - t0) > a.budget_ns) {
-          atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
-          ok = 0;
-          break;
-        }
+    if (!mbar_wait_bounded(bar, phase, a)) {
+      asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      if (mbar_test_wait(bar, phase)) {
+        asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      } else {
+        atomicCAS(&a.ctrl[1], 0, nd::kDevErrTimeout);
+        ok = 0;
       }
     }
   }
@@ -1192,6 +1230,9 @@ __global__ void __launch_bounds__(Async2Block<Store>::kThreads, 1) nomad_async2_
   CtaRegion C = cta_region(region, a.f.kpad, static_cast<int>(sizeof(Store)));
   uint32_t join_phase = 0;
   unsigned in_take = 0, in_done = 0, out_tail = 0;
+  // test hook (debug bit 1): the block's last compute warp never joins a block visit,
+  // so the others' join runs out of budget
+  const bool skip_joins = (a.debug_flags & 2) != 0 && wib == nc_live - 1;
   unsigned long long n_upd = 0, n_hops = 0, n_fail = 0;
   double esum = 0.0;
   unsigned backoff = 32;
@@ -1214,7 +1255,7 @@ __global__ void __launch_bounds__(Async2Block<Store>::kThreads, 1) nomad_async2_
         if (hv >= 0) hv = static_cast<int>(ld_acquire_cta_u32(reinterpret_cast<const unsigned*>(&hdr->hv_tok)));
       }
       hv = __shfl_sync(kFull, hv, 0);
-      if (hv >= 0) {
+      if (hv >= 0 && !skip_joins) {
         cp_async_wait<0>();  // tk0's indices land before the region is reused
         __syncwarp();
         if (!cta_join(join_bar, join_phase, a, lane)) break;

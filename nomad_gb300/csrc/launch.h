@@ -52,6 +52,7 @@ struct AsyncArgs {
   int4* mailbox = nullptr;    // [4n] next visit of each token (four int4)
   const int4* segx = nullptr; // [3 * segments] each visit followed by its first four ratings
   int32_t cta_heavy = 0;      // priority tokens visit thread blocks, whose warps process them together
+  int32_t debug_flags = 0;    // test hooks (nomad_gpu_params.debug_flags)
 };
 
 struct ReplayArgs {

@@ -290,6 +290,31 @@ def test_timeout_is_a_status_and_context_survives(ng, gpu_ok):
         assert st["updates"] == train.nnz
 
 
+def test_block_visit_join_timeout_is_a_status(ng, gpu_ok):
+    """A worker that never joins its thread block's visit of a priority column (test
+    hook, debug bit 1) leaves the block's other workers waiting at the join; their
+    bounded wait ends in NOMAD_ERR_TIMEOUT after the spin budget, every warp leaves (the
+    phase barriers inside a block visit are bounded waits as well), and the context
+    stays usable; a context without the hook trains every rating."""
+    train, test = ng.synth(ng.synth_spec(2, m=3000, n=300, nnz_train=60000, nnz_test=2000,
+                                         seed=12345))
+    p = ng.default_params(dim=32, lrate=LR, drate=DR, reg=REG, mode="async", workers=64,
+                          warps_per_block=8, priority_permille=100, spin_budget_ms=200,
+                          debug_flags=2)
+    with ng.Nomad(train, test, params=p) as nm:
+        assert nm.info()["priority_tokens"] > 0
+        for _ in range(2):
+            with pytest.raises(ng.NomadError) as ei:
+                nm.epoch(1)
+            assert ei.value.status == -4
+        assert nm.epoch(0)["epochs_done"] == 0
+        assert np.isfinite(nm.rmse()[0])
+    p.debug_flags = 0
+    with ng.Nomad(train, test, params=p) as nm2:
+        st = nm2.epoch(2)
+        assert st["updates"] == 2 * train.nnz
+
+
 def test_factor_roundtrip(ng, gpu_ok):
     train, test = small_problem(ng)
     rng = np.random.default_rng(0)

@@ -31,6 +31,9 @@ import subprocess
 import sys
 import tempfile
 import time
+import zlib
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -41,6 +44,9 @@ WORKLOAD_ID = 2
 HP = dict(dim=100, lrate=0.002, drate=0.05, reg=0.05)
 BYTES_PER_UPDATE = {"fp32": 2 * 100 * 4 + 8, "bf16": 2 * 100 * 2 + 8}  # w_i read+write, index, value
 TARGET_FILE = os.path.join(ROOT, "tests", "golden", "workload2_fp64_rmse.json")
+ASYNC_TARGET_FILE = os.path.join(ROOT, "tests", "golden", "workload2_async_fp64_rmse.json")
+W3_TARGET_FILE = os.path.join(ROOT, "tests", "golden", "workload3_fp64_rmse.json")
+HP3 = dict(dim=100, lrate=0.0005, drate=0.05, reg=0.05)  # ratings 0-100: a smaller step
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "async_kernel_traffic.json")
 
 
@@ -67,6 +73,9 @@ def parse():
                     help="netflix: the headline 480,189 x 17,770 workload; batched: the "
                          "4,096-problem batch (a separate line, not the headline)")
     ap.add_argument("--count", type=int, default=4096, help="problems in the batched workload")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the 1,000,990 x 624,961 precision workload and the batched workload "
+                         "(extra keys of the headline line)")
     ap.add_argument("--no-ttt", action="store_true",
                     help="skip the time-to-target runs (fresh contexts trained to the FP64 target)")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -158,12 +167,21 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def target_curve():
+def target_curve(path=TARGET_FILE):
     try:
-        with open(TARGET_FILE) as f:
+        with open(path) as f:
             return json.load(f)
     except OSError:
         return None
+
+
+def workload_checksum(train, test):
+    """CRC-32 over the generated rating arrays (the figure the committed FP64
+    trajectories carry, so that a curve is only used on the data it was made on)."""
+    c = 0
+    for a in (train.row_counts, train.cols, train.vals, test.row_counts, test.cols, test.vals):
+        c = zlib.crc32(np.ascontiguousarray(a).view(np.uint8), c)
+    return c
 
 
 # ---------------------------------------------------------------------------------
@@ -198,32 +216,47 @@ def run_form(ng, train, test, precision, W, K, device, args, clocks=None):
             "host_updates_per_s": upd / max(sum(x["host_s"] for x in timed), 1e-12)}
 
 
-def time_to_target(ng, train, test, form, curve, device, args, max_epochs=40):
+def time_to_target(ng, train, test, form, curves, checksum, device, args, hp=HP, max_epochs=40):
     """Device seconds of training until the test RMSE is within 0.5% of the FP64 oracle's
-    RMSE after all of its epochs (the committed 20-epoch trajectory of the same workload,
-    init and hyper-parameters): a fresh context trains epoch by epoch, reading the test
-    RMSE after each, until it reaches 1.005 x that RMSE or `max_epochs` pass.  Also the
-    gap to the oracle at equal epochs (largest, and at the oracle's last epoch)."""
-    if not curve:
+    RMSE after all of its epochs (the committed trajectories of the same workload, init
+    and hyper-parameters): a fresh context trains epoch by epoch, reading the test RMSE
+    after each, until it reaches 1.005 x that RMSE or `max_epochs` pass.  Reported
+    against each committed FP64 oracle: `replay` (nomad_double with one worker) and,
+    where committed, `async` (nomad_double with P workers, the oracle's deterministic
+    event simulation).  Per oracle: the signed relative gap (GPU - oracle) / oracle at
+    every epoch, its largest magnitude over all epochs and after the first, and the
+    epoch and seconds at which the target is reached.  A curve made on other data (its
+    workload checksum differs) is not used."""
+    curves = {k: c for k, c in curves.items() if c}
+    if not curves:
         return None
-    ref = curve["test_rmse"]
-    target = ref[-1] * 1.005
-    kw = dict(HP, precision=form, mode="async", device=device, init_parts=16,
+    bad = {k: c.get("checksum") for k, c in curves.items() if c.get("checksum") != checksum}
+    if bad:
+        return {"skipped": f"workload checksum {checksum} differs from the committed curves' {bad}"}
+    kw = dict(hp, precision=form, mode="async", device=device, init_parts=16,
               workers=args.workers, warps_per_block=args.wpb, blocks_per_sm=args.bps)
-    t, hit, hit_epochs, gaps = 0.0, None, None, []
+    need = max(len(c["test_rmse"]) for c in curves.values())
+    t, rm, secs = 0.0, [], []
     with ng.Nomad(train, test, **kw) as nm:
         for e in range(max_epochs):
             t += nm.epoch(1)["device_ms"] / 1e3
-            te = nm.rmse(train=False)[1]
-            if e < len(ref):
-                gaps.append(abs(te - ref[e]) / ref[e])
-            if te <= target:
-                hit, hit_epochs = t, e + 1
-                if e + 1 >= len(ref):
-                    break
-    return {"seconds": hit, "epochs": hit_epochs, "target_rmse": target,
-            "oracle_epochs": len(ref), "gap_at_oracle_epochs": gaps[len(ref) - 1] if len(gaps) >= len(ref) else None,
-            "max_gap": max(gaps) if gaps else None}
+            rm.append(nm.rmse(train=False)[1])
+            secs.append(t)
+            done = [rm[-1] <= c["test_rmse"][-1] * 1.005 for c in curves.values()]
+            if e + 1 >= need and all(done):
+                break
+    out = {"gpu_test_rmse": rm}
+    for k, c in curves.items():
+        ref = c["test_rmse"]
+        target = ref[-1] * 1.005
+        hit = next((i for i, x in enumerate(rm) if x <= target), None)
+        gaps = [(g - r) / r for g, r in zip(rm, ref)]
+        out[k] = {"oracle": c.get("mode"), "target_rmse": target, "oracle_epochs": len(ref),
+                  "epochs": None if hit is None else hit + 1, "seconds": None if hit is None else secs[hit],
+                  "gap_per_epoch": gaps, "max_gap": max(abs(g) for g in gaps),
+                  "max_gap_after_first": max((abs(g) for g in gaps[1:]), default=None),
+                  "gap_at_oracle_epochs": gaps[len(ref) - 1] if len(gaps) >= len(ref) else None}
+    return out
 
 
 def e2e_run(ng, train, test, K, device, args):
@@ -250,11 +283,10 @@ def e2e_run(ng, train, test, K, device, args):
 def cpu_baseline(train, seconds):
     """The oracle's asynchronous float mode (the reference's updater loop restated),
     every host core, one wall-clock interval of the same workload."""
-    import nomad_gb300 as ng
     from oracle import oracle as O
     cores = os.cpu_count() or 1
     csc = O.row_major_to_csc(train.m, train.n, train.row_counts, train.cols, train.vals)
-    W, H = ng.reference_init(train.m, train.n, HP["dim"], 12345, cores)
+    W, H = (x.astype(np.float32) for x in O.init_factors(train.m, train.n, HP["dim"], 12345, cores))
     st = O.async_train(csc, W, H, nthreads=cores, n_epochs=0, timeout_sec=seconds,
                        lrate=HP["lrate"], drate=HP["drate"], reg=HP["reg"], seed=12345)
     return {"value": st["updates"] / st["seconds"], "unit": UNIT, "cores": cores,
@@ -274,16 +306,102 @@ def config_block(K, W):
             "parallelism": "replicas"}
 
 
+def precision_workload_run(ng, device, args):
+    """The 1,000,990 x 624,961 precision workload (252.8M training ratings, Zipf(0.9)
+    degrees on both sides, integer ratings 0-100): both storage forms from the same
+    init, test RMSE after every epoch, against the committed FP64 oracle trajectory of
+    this workload.  The first epoch is a warm-up for the timing."""
+    t = time.perf_counter()
+    train, test = ng.synth(3)
+    gen_s = time.perf_counter() - t
+    checksum = workload_checksum(train, test)
+    curve = target_curve(W3_TARGET_FILE)
+    ok = bool(curve) and curve.get("checksum") == checksum
+    epochs = len(curve["test_rmse"]) if ok else 4
+    out = {"workload": "1,000,990 x 624,961, 252,800,275 train / 4,003,960 test ratings (Zipf(0.9) both "
+                       "sides, integer ratings 0-100 from a planted rank-30 model)",
+           **HP3, "workload_checksum": checksum, "generate_s": gen_s,
+           "oracle": (curve or {}).get("mode") if ok else None}
+    if curve and not ok:
+        out["oracle_skipped"] = f"workload checksum {checksum} differs from the committed curve's {curve.get('checksum')}"
+    for form in ("fp32", "bf16"):
+        t0 = time.perf_counter()
+        with ng.Nomad(train, test, precision=form, mode="async", device=device, init_parts=16, **HP3) as nm:
+            init_s = time.perf_counter() - t0
+            ms, rm = [], []
+            for _ in range(epochs):
+                ms.append(nm.epoch(1)["device_ms"])
+                rm.append(nm.rmse(train=False)[1])
+        timed = ms[1:] if len(ms) > 1 else ms
+        r = {"updates_per_s": train.nnz / (sum(timed) / len(timed) / 1e3), "ms_per_epoch": sum(timed) / len(timed),
+             "init_s": init_s, "test_rmse": rm}
+        if ok:
+            ref = curve["test_rmse"]
+            target = ref[-1] * 1.005
+            hit = next((i for i, x in enumerate(rm) if x <= target), None)
+            r["gap_per_epoch"] = [(g - o) / o for g, o in zip(rm, ref)]
+            r["max_gap"] = max(abs(g) for g in r["gap_per_epoch"])
+            r["target_rmse"] = target
+            r["epochs_to_target"] = None if hit is None else hit + 1
+            r["seconds_to_target"] = None if hit is None else sum(ms[:hit + 1]) / 1e3
+        r["roofline_frac"] = BYTES_PER_UPDATE[form] * r["updates_per_s"] / 1e9 / hbm_peak()[0]
+        out[form] = r
+        log(f"[bench] 1,000,990x624,961 {form}: {r['updates_per_s']:.4g} updates/s, {r['ms_per_epoch']:.1f} ms/epoch")
+    out["bf16_over_fp32"] = out["bf16"]["updates_per_s"] / out["fp32"]["updates_per_s"]
+    return out
+
+
+def batched_run(ng, device, K, W, count=4096):
+    """The batched form: `count` independent problems of uneven shape and rank (m in
+    [200, 20,000], n in [100, 5,000], density 0.5-5%, k in {16, 32, 64}), one CUDA-graph
+    launch per epoch; compared with looping the single-problem path over a sample."""
+    t = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:  # one generator thread each
+        probs = list(ex.map(lambda i: ng.synth_batch_problem(i, threads=1), range(count)))
+    nnz = sum(p[0].nnz for p in probs)
+    log(f"[bench] {count} problems ({nnz} train ratings) generated in {time.perf_counter() - t:.1f} s")
+    kw = dict(lrate=0.002, drate=0.1, reg=0.05, device=device)
+    res = {"workload": f"{count} problems, {nnz} train ratings: m logU[200, 20k], n logU[100, 5k], "
+                       "density logU[0.5%, 5%], k in {16, 32, 64}, planted rank k/4",
+           "lrate": 0.002, "drate": 0.1, "reg": 0.05, "steps": K, "warmup": W,
+           "step": "one epoch of every problem (one graph launch)"}
+    for form in ("fp32", "bf16"):
+        t0 = time.perf_counter()
+        b = ng.Batch(probs, precision=form, **kw)
+        init_s = time.perf_counter() - t0
+        b.epoch(W)
+        st = b.epoch(K)
+        _, te = b.rmse()
+        b.close()
+        e2e_s = time.perf_counter() - t0
+        res[form] = {"updates_per_s": st["updates"] / (st["device_ms"] / 1e3),
+                     "ms_per_epoch": st["device_ms"] / K, "init_s": init_s,
+                     "e2e_updates_per_s": (W + K) * nnz / e2e_s,
+                     "median_test_rmse": float(sorted(te)[len(te) // 2])}
+        log(f"[bench] batched {form}: {res[form]['updates_per_s']:.4g} updates/s, "
+            f"{res[form]['ms_per_epoch']:.2f} ms/epoch")
+    # looping the single-problem path (one context per problem, replay schedule) on a sample
+    upd, secs = 0, 0.0
+    for train, test, dim in probs[:64]:
+        with ng.Nomad(train, test, dim=dim, mode="replay", precision="fp32", **kw) as nm:
+            st = nm.epoch(2)
+        upd += st["updates"]
+        secs += st["device_ms"] / 1e3
+    res["looping_single_problem_path"] = {"updates_per_s": upd / secs,
+                                          "sample": "first 64 problems, fp32 replay, 2 epochs",
+                                          "batched_bf16_over_looping": res["bf16"]["updates_per_s"] / (upd / secs)}
+    return res
+
+
 # ---------------------------------------------------------------------------------
 def main_reference(args, dist):
     if dist.rank != 0:
         return
-    import nomad_gb300 as ng
-    from oracle import oracle as O
-    train, test = ng.synth(WORKLOAD_ID)
+    from oracle import oracle as O  # the oracle and the workload generator; no GPU library
+    train, _ = O.workload(WORKLOAD_ID)
     cores = os.cpu_count() or 1
-    csc = O.row_major_to_csc(train.m, train.n, train.row_counts, train.cols, train.vals)
-    W, H = ng.reference_init(train.m, train.n, HP["dim"], 12345, cores)
+    csc = O.row_major_to_csc(train["m"], train["n"], train["row_counts"], train["cols"], train["vals"])
+    W, H = (x.astype(np.float32) for x in O.init_factors(train["m"], train["n"], HP["dim"], 12345, cores))
     sample_s = max(1.0, min(10.0, 150.0 / max(args.steps + args.warmup, 1)))
     for _ in range(args.warmup):
         O.async_train(csc, W, H, nthreads=cores, timeout_sec=sample_s, lrate=HP["lrate"],
@@ -306,8 +424,10 @@ def main_reference(args, dist):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference (MPI+TBB+Boost+glog) cannot be built on these hosts; this is "
-                "the oracle's restatement of its updater loop"}), flush=True)
+        "note": "the reference's updater compiles only where its source tree is (against "
+                "stand-ins for MPI, TBB, Boost and glog); the GPU host has no copy of it, so "
+                "this is the oracle's restatement of its updater loop, inputs made by the "
+                "standalone workload generator (no GPU library loaded)"}), flush=True)
 
 
 def main_ours(args, dist):
@@ -358,8 +478,14 @@ def main_ours(args, dist):
         traffic = tr["dram_bytes_per_update"]["bf16"] * b["timed_updates"] / max(K, 1)
     except (OSError, KeyError, ValueError):
         pass
-    curve = target_curve()
-    ttt = None if args.no_ttt else {f: time_to_target(ng, train, test, f, curve, device, args) for f in forms}
+    checksum = workload_checksum(train, test)
+    curves = {"replay": target_curve(TARGET_FILE), "async": target_curve(ASYNC_TARGET_FILE)}
+    ttt = None if args.no_ttt else {f: time_to_target(ng, train, test, f, curves, checksum, device, args)
+                                    for f in forms}
+    extra = {}
+    if not args.no_extra and dist.world == 1:
+        extra["precision_workload"] = precision_workload_run(ng, device, args)
+        extra["batched"] = batched_run(ng, device, K=6, W=2)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
         "steps": K, "warmup": W, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
@@ -385,6 +511,8 @@ def main_ours(args, dist):
         "workers": b["info"]["workers"], "segments_per_epoch": b["info"]["segments"],
         "max_column": b["info"]["max_column"],
         "host_updates_per_s": b["host_updates_per_s"],
+        "workload_checksum": checksum,
+        **extra,
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(train, args.cpu_seconds)
@@ -397,52 +525,17 @@ def main_batched(args, dist):
     [200, 20,000], n in [100, 5,000], density 0.5-5%, k in {16, 32, 64}), one CUDA-graph
     launch per epoch; compared with looping the single-problem path over a sample."""
     import nomad_gb300 as ng
-    device = dist.local
     K, W = args.steps, args.warmup
-    t = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:  # one generator thread each
-        probs = list(ex.map(lambda i: ng.synth_batch_problem(i, threads=1), range(args.count)))
-    nnz = sum(p[0].nnz for p in probs)
-    log(f"[bench] {args.count} problems ({nnz} train ratings) generated in {time.perf_counter() - t:.1f} s")
-    kw = dict(lrate=0.002, drate=0.1, reg=0.05, device=device)
-    res = {}
-    for form in ("fp32", "bf16"):
-        t0 = time.perf_counter()
-        b = ng.Batch(probs, precision=form, **kw)
-        init_s = time.perf_counter() - t0
-        b.epoch(W)
-        st = b.epoch(K)
-        _, te = b.rmse()
-        b.close()
-        e2e_s = time.perf_counter() - t0
-        res[form] = {"updates_per_s": st["updates"] / (st["device_ms"] / 1e3),
-                     "ms_per_epoch": st["device_ms"] / K, "init_s": init_s,
-                     "e2e_updates_per_s": (W + K) * nnz / e2e_s,
-                     "median_test_rmse": float(sorted(te)[len(te) // 2])}
-        log(f"[bench] batched {form}: {res[form]['updates_per_s']:.4g} updates/s, "
-            f"{res[form]['ms_per_epoch']:.2f} ms/epoch")
-    # looping the single-problem path (one context per problem, replay schedule) on a sample
-    sample = probs[:64]
-    upd, secs = 0, 0.0
-    for train, test, dim in sample:
-        with ng.Nomad(train, test, dim=dim, mode="replay", precision="fp32", **kw) as nm:
-            st = nm.epoch(2)
-        upd += st["updates"]
-        secs += st["device_ms"] / 1e3
-    loop = upd / secs
+    res = batched_run(ng, dist.local, K, W, args.count)
     b = res["bf16"]
     print(json.dumps({
         "metric": "aggregate rating updates/s, batched independent problems", "value": b["updates_per_s"],
         "unit": UNIT, "n_gpus": dist.world, "steps": K, "warmup": W, "ms_per_step": b["ms_per_epoch"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
         "data": "synthetic (seeded batched workload)",
-        "config": {"workload": f"{args.count} problems, {nnz} train ratings: m logU[200, 20k], n logU[100, 5k], "
-                               "density logU[0.5%, 5%], k in {16, 32, 64}, planted rank k/4",
-                   "lrate": 0.002, "drate": 0.1, "reg": 0.05,
-                   "step": "one epoch of every problem (one graph launch)"},
+        "config": {k: res[k] for k in ("workload", "lrate", "drate", "reg", "step")},
         "fp32": res["fp32"], "bf16": res["bf16"],
-        "looping_single_problem_path": {"updates_per_s": loop, "sample": "first 64 problems, fp32 replay, 2 epochs",
-                                        "batched_over_looping": b["updates_per_s"] / loop},
+        "looping_single_problem_path": res["looping_single_problem_path"],
         "e2e": {"value": b["e2e_updates_per_s"], "unit": UNIT}}), flush=True)
 
 

@@ -322,3 +322,40 @@ def async_sim(csc, W, H, P, first_epoch, n_epochs, lrate, drate, reg, seed=12345
     _check(f(m, n, dim, _p(col_ptr), _p(row_idx), _p(vals), _p(W), _p(H), P, partition, first_epoch,
              n_epochs, lrate, drate, reg, seed, visit_cost, rating_cost, hop_cost, _p(err)), "async_sim")
     return err[:n_epochs]
+
+
+# ---- the seeded workloads, without the GPU library ---------------------------------
+_WL_LIB_PATH = os.path.join(_HERE, "_build", "libnomad_workload.so")
+
+
+def workload(workload_id, **overrides):
+    """The library's seeded synthetic workload `workload_id` (nomad_synth_preset /
+    nomad_synth_generate), generated by the same host code built on its own
+    (oracle/_build/libnomad_workload.so), so that a CPU-only run needs no GPU library.
+    Returns (train, test), each a dict of m, n, row_counts, cols, vals."""
+    from nomad_gb300 import _abi  # ctypes structures only; loads no library
+    if not os.path.exists(_WL_LIB_PATH):
+        build()
+    L = ctypes.CDLL(_WL_LIB_PATH)
+    L.nomad_synth_preset.restype = ctypes.c_int
+    L.nomad_synth_preset.argtypes = [_i32, ctypes.POINTER(_abi.SynthSpec)]
+    L.nomad_synth_generate.restype = ctypes.c_int
+    L.nomad_synth_generate.argtypes = [ctypes.POINTER(_abi.SynthSpec), ctypes.POINTER(_abi.IoMatrix),
+                                       ctypes.POINTER(_abi.IoMatrix)]
+    L.nomad_io_free.restype = None
+    L.nomad_io_free.argtypes = [ctypes.POINTER(_abi.IoMatrix)]
+    spec = _abi.SynthSpec()
+    _check(L.nomad_synth_preset(int(workload_id), ctypes.byref(spec)), "nomad_synth_preset")
+    for k, v in overrides.items():
+        setattr(spec, k, v)
+    tr, te = _abi.IoMatrix(), _abi.IoMatrix()
+    _check(L.nomad_synth_generate(ctypes.byref(spec), ctypes.byref(tr), ctypes.byref(te)), "nomad_synth_generate")
+    out = []
+    for io in (tr, te):
+        d = {"m": io.m, "n": io.n,
+             "row_counts": np.ctypeslib.as_array(io.row_counts, (io.m,)).copy() if io.m else np.zeros(0, np.int32),
+             "cols": np.ctypeslib.as_array(io.cols, (io.nnz,)).copy() if io.nnz else np.zeros(0, np.int32),
+             "vals": np.ctypeslib.as_array(io.vals, (io.nnz,)).copy() if io.nnz else np.zeros(0)}
+        L.nomad_io_free(ctypes.byref(io))
+        out.append(d)
+    return out[0], out[1]

@@ -104,7 +104,11 @@ typedef struct nomad_gpu_params {
                           largest column's ratings use the workers' priority queues;
                           0 = default 50, negative = no priority queue                */
   int32_t lr_strategy; /* nomad_gpu_lr_strategy (BOLD_DRIVER: DSGD and DSGDPP)  FIXED */
-  int32_t reserved[5];
+  int32_t batch_share; /* batched form (exact = 0): a problem with at least this many
+                          times one warp's fair share of the batch's ratings (and at
+                          least 8,192) runs on a whole thread block of NOMAD workers;
+                          0 = default 4, negative = every problem on one warp        */
+  int32_t reserved[4];
 } nomad_gpu_params;
 
 /* One rating set in either the reference's row-major file layout (row_counts !=
@@ -325,6 +329,25 @@ int nomad_gpu_batch_init(nomad_gpu_batch** out, const nomad_gpu_batch_problem* p
 /* n_epochs epochs of every problem; st->updates sums over problems, device_ms times the
  * graph launches (CUDA events). */
 int nomad_gpu_batch_epoch(nomad_gpu_batch* b, int32_t n_epochs, nomad_gpu_epoch_stats* st);
+/* One configuration tried by nomad_gpu_batch_autotune and its mean device time per epoch. */
+typedef struct nomad_gpu_batch_tune_trial {
+  int32_t batch_share;  /* large-problem threshold (params.batch_share)            */
+  int32_t status;       /* NOMAD_OK, or the status the trial ended with             */
+  double device_ms;     /* mean device time of the timed epochs                     */
+  int32_t large_problems; /* problems that ran on whole thread blocks               */
+  int32_t reserved;
+} nomad_gpu_batch_tune_trial;
+
+/* Chooses the batched form's large-problem threshold (params.batch_share) for these
+ * problems by measurement: shares 2, 4, 8, 16 and "never", each a fresh batch from
+ * params, one untimed epoch and `epochs` timed ones (the factors are discarded).  On
+ * success params->batch_share holds the fastest share and trials[0 .. *n_trials) the
+ * measurements.  NOMAD_ERR_UNSUPPORTED for exact = 1 (one warp per problem).  No
+ * counterpart in the reference (it trains one problem per run). */
+int nomad_gpu_batch_autotune(const nomad_gpu_batch_problem* problems, int32_t count, nomad_gpu_params* params,
+                             int32_t epochs, nomad_gpu_batch_tune_trial* trials, int32_t max_trials,
+                             int32_t* n_trials);
+
 /* Per-problem RMSE (FP64 sums), arrays of `count` doubles; a problem without ratings in a
  * set gets 0. */
 int nomad_gpu_batch_rmse(nomad_gpu_batch* b, double* train_rmse, double* test_rmse);

@@ -220,6 +220,39 @@ def autotune(train, test=None, epochs=1, W0=None, H0=None, **kw):
     return best, [{k: getattr(t, k) for k, _ in _abi.TuneTrial._fields_} for t in trials[:n.value]]
 
 
+def _batch_problems(problems):
+    """ctypes array of nomad_gpu_batch_problem for (train, test, dim[, W0, H0]) tuples, and
+    the arrays it points into (keep them alive while the array is used)."""
+    arr = (_abi.BatchProblem * len(problems))()
+    keep = []
+    for i, prob in enumerate(problems):
+        train, test, dim = prob[0], prob[1], int(prob[2])
+        W0 = H0 = None
+        if len(prob) > 3 and prob[3] is not None:
+            W0 = np.ascontiguousarray(prob[3], np.float32)
+        if len(prob) > 4 and prob[4] is not None:
+            H0 = np.ascontiguousarray(prob[4], np.float32)
+        keep += [train, test, W0, H0]
+        arr[i] = _abi.BatchProblem(train.m, train.n, dim, 0, train._c(), test._c(), _ptr(W0), _ptr(H0))
+    return arr, keep
+
+
+def batch_autotune(problems, epochs=1, **kw):
+    """Measured choice of the batched form's large-problem threshold for these problems
+    (nomad_gpu_batch_autotune): returns (keyword arguments for Batch with batch_share set,
+    list of the trials with their ms per epoch and large-problem counts)."""
+    p = default_params(**kw)
+    arr, keep = _batch_problems(problems)
+    trials = (_abi.BatchTuneTrial * 16)()
+    n = ctypes.c_int32()
+    check(lib().nomad_gpu_batch_autotune(arr, len(problems), ctypes.byref(p), epochs, trials, 16,
+                                         ctypes.byref(n)), "nomad_gpu_batch_autotune")
+    del keep
+    best = dict(kw, batch_share=p.batch_share)
+    return best, [{k: getattr(t, k) for k, _ in _abi.BatchTuneTrial._fields_ if k != "reserved"}
+                  for t in trials[:n.value]]
+
+
 class Nomad:
     """One training context on the GPU (nomad_gpu_ctx)."""
 
@@ -331,19 +364,8 @@ class Batch:
         self._b = ctypes.c_void_p()
         p = params if params is not None else default_params(**kw)
         self.params = p
-        self.shapes = []
-        arr = (_abi.BatchProblem * len(problems))()
-        self._keep = []
-        for i, prob in enumerate(problems):
-            train, test, dim = prob[0], prob[1], int(prob[2])
-            W0 = H0 = None
-            if len(prob) > 3 and prob[3] is not None:
-                W0 = np.ascontiguousarray(prob[3], np.float32)
-            if len(prob) > 4 and prob[4] is not None:
-                H0 = np.ascontiguousarray(prob[4], np.float32)
-            self._keep += [train, test, W0, H0]
-            arr[i] = _abi.BatchProblem(train.m, train.n, dim, 0, train._c(), test._c(), _ptr(W0), _ptr(H0))
-            self.shapes.append((train.m, train.n, dim))
+        self.shapes = [(prob[0].m, prob[0].n, int(prob[2])) for prob in problems]
+        arr, self._keep = _batch_problems(problems)
         check(lib().nomad_gpu_batch_init(ctypes.byref(self._b), arr, len(problems), ctypes.byref(p)),
               "nomad_gpu_batch_init")
         self._keep = None  # the library copied the host arrays

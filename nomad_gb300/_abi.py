@@ -44,7 +44,8 @@ class Params(ctypes.Structure):
                 ("warps_per_block", c_i32), ("blocks_per_sm", c_i32), ("balance", c_i32),
                 ("dsgd_inner_blocks", c_i32), ("dsgd_strategy", c_i32), ("exact", c_i32),
                 ("spin_budget_ms", c_i32), ("debug_flags", c_i32), ("long_visit", c_i32),
-                ("priority_permille", c_i32), ("lr_strategy", c_i32), ("reserved", c_i32 * 5)]
+                ("priority_permille", c_i32), ("lr_strategy", c_i32), ("batch_share", c_i32),
+                ("reserved", c_i32 * 4)]
 
 
 class Matrix(ctypes.Structure):
@@ -72,6 +73,11 @@ class EpochStats(ctypes.Structure):
 class TuneTrial(ctypes.Structure):
     _fields_ = [("warps_per_block", c_i32), ("priority_permille", c_i32), ("long_visit", c_i32),
                 ("status", c_i32), ("device_ms", c_dbl)]
+
+
+class BatchTuneTrial(ctypes.Structure):
+    _fields_ = [("batch_share", c_i32), ("status", c_i32), ("device_ms", c_dbl),
+                ("large_problems", c_i32), ("reserved", c_i32)]
 
 
 class CheckpointInfo(ctypes.Structure):
@@ -128,6 +134,9 @@ SIGNATURES = {
     "nomad_gpu_token_finish_times": (ctypes.c_int, [c_vp, c_vp]),
     "nomad_gpu_autotune": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params), c_i32,
                                           ctypes.POINTER(TuneTrial), c_i32, ctypes.POINTER(c_i32)]),
+    "nomad_gpu_batch_autotune": (ctypes.c_int, [ctypes.POINTER(BatchProblem), c_i32, ctypes.POINTER(Params),
+                                                c_i32, ctypes.POINTER(BatchTuneTrial), c_i32,
+                                                ctypes.POINTER(c_i32)]),
     "nomad_gpu_sse_noalloc": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,
                                              c_i64, c_i32, c_vp, c_vp]),
     "nomad_gpu_batch_init": (ctypes.c_int, [ctypes.POINTER(c_vp), ctypes.POINTER(BatchProblem), c_i32,

@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -15,6 +16,7 @@
 #include "launch.h"
 #include "layout.h"
 #include "trace.h"
+#include "tune.h"
 
 struct nomad_gpu_batch {
   nomad_gpu_params prm{};
@@ -30,6 +32,7 @@ struct nomad_gpu_batch {
   int32_t n_steps = 0, epochs_done = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  int32_t n_big = 0;  // problems on whole thread blocks
 };
 
 namespace {
@@ -213,8 +216,9 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   std::vector<int32_t> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return nnz[x] > nnz[y]; });
-  // FMA form: problems with more than four warps' fair share of the ratings run on a whole
-  // block as NOMAD workers (rows split into kBatchWorkers blocks of equal rating counts)
+  // FMA form: problems with more than `batch_share` (default 4) warps' fair share of the
+  // ratings run on a whole block as NOMAD workers (rows split into kBatchWorkers blocks of
+  // equal rating counts)
   int bps = 0;
   if (p.exact)
     CK(nomad::batch_occupancy(bf16, 1, &bps));
@@ -224,7 +228,9 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   b->grid = bps * b->num_sms;
   const int64_t total = std::accumulate(nnz.begin(), nnz.end(), int64_t(0));
   const int64_t warps = static_cast<int64_t>(b->grid) * (p.exact ? nomad::kBatchThreads / 32 : nomad::kBatchWorkers);
-  const int64_t big_min = std::max<int64_t>(8192, 4 * total / std::max<int64_t>(warps, 1));
+  const int64_t share = p.batch_share == 0 ? 4 : p.batch_share;
+  const int64_t big_min = share < 0 ? std::numeric_limits<int64_t>::max()
+                                    : std::max<int64_t>(8192, share * total / std::max<int64_t>(warps, 1));
   int32_t n_big = 0;
   constexpr int R = nomad::kBatchWorkers;
   std::vector<int32_t> rs_all;
@@ -309,6 +315,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   RC(dalloc(b, &a.sse, 4 * static_cast<size_t>(count)));
   CK(cudaMemsetAsync(a.epoch, 0, sizeof(int32_t), b->stream));
   a.n_big = n_big;
+  b->n_big = n_big;
   RC(dalloc(b, &a.next_big, 1));
   RC(dalloc(b, &a.ctrl, 2));
   CK(cudaMemsetAsync(a.next_big, 0, sizeof(int32_t), b->stream));
@@ -500,6 +507,43 @@ int nomad_gpu_batch_get_factors(nomad_gpu_batch* b, int32_t problem, float* W, f
 void nomad_gpu_batch_destroy(nomad_gpu_batch* b) {
   if (b) cudaSetDevice(b->device);
   release(b);
+}
+
+int nomad_gpu_batch_autotune(const nomad_gpu_batch_problem* problems, int32_t count, nomad_gpu_params* params,
+                             int32_t epochs, nomad_gpu_batch_tune_trial* trials, int32_t max_trials,
+                             int32_t* n_trials) {
+  nomad::clear_last_error();
+  if (!problems || count <= 0 || !params || epochs < 1 || max_trials < 0 || (max_trials > 0 && !trials))
+    NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "invalid arguments to nomad_gpu_batch_autotune");
+  if (params->exact) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "exact = 1 runs every problem on one warp: nothing to tune");
+  if (n_trials) *n_trials = 0;
+  std::vector<nomad_gpu_batch_tune_trial> done;
+  // one trial: a fresh batch, an untimed epoch, `epochs` timed ones
+  auto measure = [&](nomad_gpu_batch_tune_trial& t) {
+    nomad_gpu_params q = *params;
+    q.batch_share = t.batch_share;
+    nomad_gpu_batch* b = nullptr;
+    t.status = nomad_gpu_batch_init(&b, problems, count, &q);
+    if (t.status == NOMAD_OK) {
+      nomad_gpu_epoch_stats st;
+      t.status = nomad_gpu_batch_epoch(b, 1, &st);
+      if (t.status == NOMAD_OK) t.status = nomad_gpu_batch_epoch(b, epochs, &st);
+      if (t.status == NOMAD_OK) {
+        t.device_ms = st.device_ms / epochs;
+        t.large_problems = b->n_big;
+      }
+    }
+    nomad_gpu_batch_destroy(b);
+  };
+  int32_t share = 0;
+  const bool ok = nomad::batch_share_search(params->batch_share, measure, done, &share);
+  const int32_t stored = std::min<int32_t>(max_trials, static_cast<int32_t>(done.size()));
+  for (int32_t i = 0; i < stored; ++i) trials[i] = done[i];
+  if (n_trials) *n_trials = stored;
+  if (!ok) NOMAD_FAIL(done.front().status, "no large-problem threshold completed an epoch");
+  params->batch_share = share;
+  nomad::clear_last_error();  // a trial that failed left its detail behind
+  return NOMAD_OK;
 }
 
 }  // extern "C"

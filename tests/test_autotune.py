@@ -1,7 +1,8 @@
 """nomad_gpu_autotune: the measured choice of the ASYNC kernel's runtime configuration
 (warps per block, priority threshold, long-visit length) by coordinate descent over fresh
-contexts.  Checked: the trials it reports ran, the configuration it returns is the
-fastest of them, training with it updates every rating, and other modes are refused."""
+contexts; nomad_gpu_batch_autotune: the batched form's large-problem threshold.  Checked:
+the trials they report ran, the configuration returned is the fastest of them, training
+with it updates every rating, and what they cannot tune is refused."""
 import os
 import shutil
 import subprocess
@@ -58,3 +59,32 @@ def test_search_on_synthetic_costs(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "tune ok" in r.stdout
+
+
+@pytest.mark.gpu
+def test_batch_autotune_picks_the_fastest_share(ng, gpu_ok):
+    problems = [ng.synth_batch_problem(i, threads=1) for i in range(96)]
+    best, trials = ng.batch_autotune(problems, epochs=2, lrate=0.002, drate=0.1, reg=0.05)
+    assert [t["batch_share"] for t in trials] == [4, 2, 8, 16, -1]
+    assert all(t["status"] == 0 and t["device_ms"] > 0 for t in trials)
+    assert trials[-1]["large_problems"] == 0          # "never": every problem on one warp
+    assert trials[1]["large_problems"] >= trials[2]["large_problems"] >= trials[3]["large_problems"]
+    fastest = min(trials, key=lambda t: t["device_ms"])
+    assert best["batch_share"] == fastest["batch_share"]
+    nnz = sum(p[0].nnz for p in problems)
+    with ng.Batch(problems, **best) as b:
+        assert b.epoch(1)["updates"] == nnz
+
+
+def test_batch_autotune_refusals(ng):
+    """Checked before any device work, so this runs without a GPU."""
+    problems = [ng.synth_batch_problem(i, threads=1) for i in range(2)]
+    with pytest.raises(ng.NomadError) as e:
+        ng.batch_autotune(problems, exact=1)
+    assert e.value.status == -9
+    with pytest.raises(ng.NomadError) as e:
+        ng.batch_autotune(problems, epochs=0)
+    assert e.value.status == -1
+    with pytest.raises(ng.NomadError) as e:
+        ng.batch_autotune([])
+    assert e.value.status == -1

@@ -89,9 +89,57 @@ void case_small_blocks() {  // two warps per block: no trial below one warp
   for (const auto& t : done) CHECK(t.warps_per_block >= 1);
 }
 
+// The batched threshold search against a synthetic cost with its minimum at `best`.
+struct BatchModel {
+  int best;
+  int fail_share = 999;
+  int calls = 0;
+  void operator()(nomad_gpu_batch_tune_trial& t) {
+    ++calls;
+    if (t.batch_share == fail_share) {
+      t.status = NOMAD_ERR_OOM;
+      return;
+    }
+    const int s = t.batch_share < 0 ? 64 : t.batch_share;
+    const int b = best < 0 ? 64 : best;
+    t.device_ms = 10.0 + (s > b ? s - b : b - s);
+    t.large_problems = t.batch_share < 0 ? 0 : 100 / s;
+  }
+};
+
+void case_batch_share() {
+  std::vector<nomad_gpu_batch_tune_trial> done;
+  int32_t share = 0;
+  BatchModel m{8};
+  CHECK(nomad::batch_share_search(0, m, done, &share));
+  CHECK(share == 8 && m.calls == 5 && done.size() == 5);
+  CHECK(done[0].batch_share == 4);  // the default first
+  for (size_t i = 0; i < done.size(); ++i)
+    for (size_t j = i + 1; j < done.size(); ++j) CHECK(done[i].batch_share != done[j].batch_share);
+  done.clear();
+  BatchModel never_big{-1};
+  CHECK(nomad::batch_share_search(0, never_big, done, &share));
+  CHECK(share == -1 && done.back().large_problems == 0);
+  done.clear();
+  BatchModel odd{3};  // a starting share outside the list is measured too
+  CHECK(nomad::batch_share_search(3, odd, done, &share));
+  CHECK(share == 3 && done.size() == 6 && done[0].batch_share == 3);
+  done.clear();
+  BatchModel failing{2};
+  failing.fail_share = 2;  // the best share fails: the next best wins
+  CHECK(nomad::batch_share_search(0, failing, done, &share));
+  CHECK(share == 4);
+  struct Never {
+    void operator()(nomad_gpu_batch_tune_trial& t) { t.status = NOMAD_ERR_TIMEOUT; }
+  } never;
+  done.clear();
+  CHECK(!nomad::batch_share_search(0, never, done, &share));
+}
+
 }  // namespace
 
 int main() {
+  case_batch_share();
   case_descent();
   case_defaults_kept();
   case_failures();

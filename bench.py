@@ -70,13 +70,14 @@ def parse():
     ap.add_argument("--bps", type=int, default=0)
     ap.add_argument("--forms", default="fp32,bf16",
                     help="storage forms to run (the headline is bf16; profiling runs pick one)")
-    ap.add_argument("--workload", choices=["netflix", "batched"], default="netflix",
+    ap.add_argument("--workload", choices=["netflix", "batched", "memory"], default="netflix",
                     help="netflix: the headline 480,189 x 17,770 workload; batched: the "
-                         "4,096-problem batch (a separate line, not the headline)")
+                         "4,096-problem batch; memory: the 2.74e9-rating workload (--scale "
+                         "shrinks it for profiling); the last two print a separate line")
     ap.add_argument("--count", type=int, default=4096, help="problems in the batched workload")
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the 1,000,990 x 624,961 precision workload and the batched workload "
-                         "(extra keys of the headline line)")
+                    help="skip the 1,000,990 x 624,961 precision workload, the batched workload and "
+                         "the 2.74e9-rating memory-scale workload (extra keys of the headline line)")
     ap.add_argument("--no-ttt", action="store_true",
                     help="skip the time-to-target runs (fresh contexts trained to the FP64 target)")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -354,6 +355,63 @@ def precision_workload_run(ng, device, args):
     return out
 
 
+def host_mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 0.0
+
+
+def memory_workload_run(ng, device, epochs=2, need_gb=150.0, scale=1.0, forms=("bf16", "fp32")):
+    """The memory-scale workload: 50,082,603 x 39,780 with 2.74e9 training and 3.0e7 test
+    ratings (item degrees Zipf(1.0), user degrees geometric with mean 55, real-valued
+    ratings from a planted rank-50 model), k = 100, both storage forms: ~10 GB of bf16 /
+    ~20 GB of fp32 factors and 22 GB of ratings on the device, W far larger than L2.
+    Set-up needs ~60 GB of host memory (the generated file layout, then the CSC build);
+    the run is skipped, with the reason, when the host has less than `need_gb` free.
+    `scale` < 1 shrinks rows, columns and ratings alike (profiling captures of a smaller
+    case of the same shape)."""
+    avail = host_mem_available_gb()
+    need_gb *= scale
+    out = {"workload": "50,082,603 x 39,780, 2,740,000,000 train / 30,000,000 test ratings (Zipf(1.0) items, "
+                       "geometric(55) users, planted rank 50 + N(0, 0.2^2))",
+           "dim": 100, "lrate": 0.002, "drate": 0.05, "reg": 0.05, "host_mem_available_gb": avail}
+    if avail < need_gb:
+        out["skipped"] = f"{avail:.0f} GB of host memory free, {need_gb:.0f} GB wanted for the set-up"
+        return out
+    t = time.perf_counter()
+    if scale == 1.0:
+        train, test = ng.synth(4)
+    else:
+        out["scale"] = scale
+        train, test = ng.synth(ng.synth_spec(4, m=int(50082603 * scale), n=int(39780 * scale),
+                                             nnz_train=int(2740000000 * scale), nnz_test=int(30000000 * scale)))
+    out["generate_s"] = time.perf_counter() - t
+    for form in forms:
+        t0 = time.perf_counter()
+        with ng.Nomad(train, test, precision=form, mode="async", device=device, init_parts=16,
+                      dim=100, lrate=0.002, drate=0.05, reg=0.05) as nm:
+            init_s = time.perf_counter() - t0
+            info = nm.info()
+            ms, rm = [], []
+            for _ in range(epochs):
+                ms.append(nm.epoch(1)["device_ms"])
+                rm.append(nm.rmse(train=False)[1])
+        ups = train.nnz / (sum(ms) / len(ms) / 1e3)
+        out[form] = {"updates_per_s": ups, "ms_per_epoch": sum(ms) / len(ms), "init_s": init_s,
+                     "test_rmse": rm, "device_bytes": info["device_bytes"], "max_column": info["max_column"],
+                     "roofline_frac": BYTES_PER_UPDATE[form] * ups / 1e9 / hbm_peak()[0]}
+        log(f"[bench] 50,082,603x39,780 {form}: {ups:.4g} updates/s, {out[form]['ms_per_epoch']:.0f} ms/epoch")
+    del train, test
+    if "bf16" in out and "fp32" in out:
+        out["bf16_over_fp32"] = out["bf16"]["updates_per_s"] / out["fp32"]["updates_per_s"]
+    return out
+
+
 def batched_run(ng, device, K, W, count=4096):
     """The batched form: `count` independent problems of uneven shape and rank (m in
     [200, 20,000], n in [100, 5,000], density 0.5-5%, k in {16, 32, 64}), one CUDA-graph
@@ -489,6 +547,7 @@ def main_ours(args, dist):
     if not args.no_extra and dist.world == 1:
         extra["precision_workload"] = precision_workload_run(ng, device, args)
         extra["batched"] = batched_run(ng, device, K=6, W=2)
+        extra["memory_workload"] = memory_workload_run(ng, device)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
         "steps": K, "warmup": W, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
@@ -550,6 +609,11 @@ def main():
             main_reference(args, dist)
         elif args.workload == "batched":
             main_batched(args, dist)
+        elif args.workload == "memory":
+            import nomad_gb300 as ng
+            forms = tuple(f for f in ("bf16", "fp32") if f in args.forms.split(","))
+            print(json.dumps(memory_workload_run(ng, dist.local, epochs=max(args.steps, 1), scale=args.scale,
+                                                 forms=forms)), flush=True)
         else:
             main_ours(args, dist)
     finally:

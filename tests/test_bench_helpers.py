@@ -52,3 +52,16 @@ def test_hbm_peak_denominator():
     assert peak > 1000
     if kind == "fallback":
         assert peak == 6800.0
+
+
+def test_memory_workload_is_skipped_without_host_memory(monkeypatch):
+    """The 2.74e9-rating set-up needs ~60 GB of host memory: with too little free the bench
+    records why and generates nothing (no library call is made)."""
+    monkeypatch.setattr(bench, "host_mem_available_gb", lambda: 20.0)
+    out = bench.memory_workload_run(None, 0)
+    assert "skipped" in out and "generate_s" not in out
+    assert bench.host_mem_available_gb.__call__() == 20.0
+
+
+def test_host_memory_reading():
+    assert bench.host_mem_available_gb() >= 0.0

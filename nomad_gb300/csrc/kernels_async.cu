@@ -558,27 +558,48 @@ __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) 
   lo = tf32_bits(x - __uint_as_float(hi));
 }
 
+// Fragments by ldmatrix: each 8x8 b16 matrix is 8 rows of 16 bytes, so for 32-bit data it
+// is 8 rows x 4 words and thread l receives row l/4, word l%4 -- the layout of the mma
+// fragments below for tf32 (words) and bf16 (pairs).  One instruction replaces four (x4)
+// or two (x2) shared-memory loads per lane; lanes 0-7, 8-15, 16-23, 24-31 give the row
+// addresses of matrices 0..3 (16-byte aligned: rows are multiples of 16 bytes apart and
+// start at multiples of 4 words).
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t (&r)[4]) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr)
+               : "memory");
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t addr, uint32_t (&r)[2]) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(addr)
+               : "memory");
+}
+
 // One 16x8 tile of G = X X^T: rows r0.., columns n0.. (fragment layouts of mma.m16n8k8 /
 // m16n8k16: g = lane / 4 selects the row, t = lane % 4 the k pair or k element).  fp32
 // rows: 3xTF32, three mma per k step (hi*hi into one accumulator, hi*lo + lo*hi into
 // another, summed at the end), so G carries close to fp32 precision like the rest of
 // the fp32 form; b = X h is computed separately in fp32.
 __device__ __forceinline__ void gram_tile(const float* X, int sw, int kpad, int r0, int n0, float (&d)[4], int lane) {
-  const int g = lane >> 2, t = lane & 3;
-  const float* A0 = X + (r0 + g) * sw;
-  const float* A1 = A0 + 8 * sw;
-  const float* B = X + (n0 + g) * sw;
+  const int rr = lane & 7, mi = lane >> 3;
+  // A: matrices (rows r0.., words k0..), (rows r0+8.., k0..), (r0.., k0+4..), (r0+8.., k0+4..)
+  const uint32_t a_addr = smem_u32(X + (r0 + rr + (mi & 1) * 8) * sw + (mi >> 1) * 4);
+  // B: matrices (rows n0.., words k0..), (rows n0.., k0+4..) from lanes 0..15
+  const uint32_t b_addr = smem_u32(X + (n0 + rr) * sw + (mi & 1) * 4);
   float d2[4] = {0.f, 0.f, 0.f, 0.f};  // the cross terms hi*lo + lo*hi
   const int kmma = (kpad + 7) / 8 * 8;  // the row padded with zeros to whole k8 steps
 #pragma unroll 2
   for (int k0 = 0; k0 < kmma; k0 += 8) {
+    uint32_t ar[4], br[2];
+    ldsm_x4(a_addr + 4u * k0, ar);
+    ldsm_x2(b_addr + 4u * k0, br);
     uint32_t ah[4], al[4], bh[2], bl[2];
-    split_tf32(A0[k0 + t], ah[0], al[0]);
-    split_tf32(A1[k0 + t], ah[1], al[1]);
-    split_tf32(A0[k0 + t + 4], ah[2], al[2]);
-    split_tf32(A1[k0 + t + 4], ah[3], al[3]);
-    split_tf32(B[k0 + t], bh[0], bl[0]);
-    split_tf32(B[k0 + t + 4], bh[1], bl[1]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) split_tf32(__uint_as_float(ar[q]), ah[q], al[q]);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) split_tf32(__uint_as_float(br[q]), bh[q], bl[q]);
     mma_tf32(d2, ah, bl);
     mma_tf32(d2, al, bh);
     mma_tf32(d, ah, bh);
@@ -588,29 +609,35 @@ __device__ __forceinline__ void gram_tile(const float* X, int sw, int kpad, int 
 }
 __device__ __forceinline__ void gram_tile(const __nv_bfloat16* X, int sw, int kpad, int r0, int n0, float (&d)[4],
                                           int lane) {
-  const int g = lane >> 2, t = lane & 3;
-  const uint32_t* A0 = reinterpret_cast<const uint32_t*>(X) + (r0 + g) * sw;
-  const uint32_t* A1 = A0 + 8 * sw;
-  const uint32_t* B = reinterpret_cast<const uint32_t*>(X) + (n0 + g) * sw;
+  const int g = lane >> 2, t = lane & 3, rr = lane & 7, mi = lane >> 3;
+  const uint32_t* Xw = reinterpret_cast<const uint32_t*>(X);
+  const uint32_t a_addr = smem_u32(Xw + (r0 + rr + (mi & 1) * 8) * sw + (mi >> 1) * 4);
+  const uint32_t b_addr = smem_u32(Xw + (n0 + rr) * sw + (mi & 1) * 4);
   const int kw = kpad / 2;  // words per row; a multiple of 4
   float d2[4] = {0.f, 0.f, 0.f, 0.f};
   int k = 0;
 #pragma unroll 2
   for (; k + 16 <= kw; k += 16) {
-    const uint32_t a[4] = {A0[k + t], A1[k + t], A0[k + 4 + t], A1[k + 4 + t]};
-    const uint32_t b[2] = {B[k + t], B[k + 4 + t]};
-    const uint32_t a2[4] = {A0[k + 8 + t], A1[k + 8 + t], A0[k + 12 + t], A1[k + 12 + t]};
-    const uint32_t b2[2] = {B[k + 8 + t], B[k + 12 + t]};
+    uint32_t a[4], b[2], a2[4], b2[2];
+    ldsm_x4(a_addr + 4u * k, a);
+    ldsm_x2(b_addr + 4u * k, b);
+    ldsm_x4(a_addr + 4u * (k + 8), a2);
+    ldsm_x2(b_addr + 4u * (k + 8), b2);
     mma_bf16_k16(d, a, b);
     mma_bf16_k16(d2, a2, b2);
   }
   if (k + 8 <= kw) {
-    const uint32_t a[4] = {A0[k + t], A1[k + t], A0[k + 4 + t], A1[k + 4 + t]};
-    const uint32_t b[2] = {B[k + t], B[k + 4 + t]};
+    uint32_t a[4], b[2];
+    ldsm_x4(a_addr + 4u * k, a);
+    ldsm_x2(b_addr + 4u * k, b);
     mma_bf16_k16(d, a, b);
     k += 8;
   }
-  if (k < kw) mma_bf16_k8(d2, A0[k + t], A1[k + t], B[k + t]);
+  if (k < kw) {
+    const uint32_t* A0 = Xw + (r0 + g) * sw;
+    const uint32_t* B = Xw + (n0 + g) * sw;
+    mma_bf16_k8(d2, A0[k + t], A0[8 * sw + k + t], B[k + t]);
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) d[i] += d2[i];
 }

@@ -813,7 +813,8 @@ struct CtaVisitOut {
   int len;
 };
 
-// Rows of block b of the visit into its shared-memory slot (each warp some rows).
+// Rows of block b of the visit into its shared-memory slot (warp wib of nw warps copies
+// rows wib, wib + nw, ...).
 __device__ __forceinline__ void cta_stage_rows(const CtaRegion& C, int b, int len, const void* W, int row_bytes,
                                                int nw, int wib, int lane) {
   const int2* rvb = C.rv + (b % kHRv) * kHB;
@@ -891,9 +892,6 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
     bar_sync_named(nthr);
     const float* hcur = C.h + (i & 1) * kpad;
     float* hnext = C.h + ((i + 1) & 1) * kpad;
-    if (i + 2 < nblk) cta_stage_rows(C, i + 2, len, W, s.row_bytes, nw, wib, lane);
-    if (i + 4 < nblk) cta_stage_rv(C, i + 4, start, len, a.ratings, tid, nthr);
-    cp_async_commit();
     const char* X = C.rows + static_cast<size_t>(i % kHStages) * kHB * C.sw * 4;
     const int2* rvb = C.rv + (i % kHRv) * kHB;
     const int nr = min(kHB, len - i * kHB);
@@ -916,7 +914,17 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
       }
     }
     bar_sync_named(nthr);
+    // While warp 0 runs the chain, the other warps issue the copies of block i + 2's rows
+    // and block i + 4's indices (issuing them took 900-2,000 cycles per warp, which at
+    // the start of the block delayed the Gram tiles); with one warp, warp 0 issues them
+    // after the chain.  Each thread commits one copy group per block either way.
     if (wib == 0) e2 += cta_chain(C.G, C.bsh, rvb, C.nesh, nr, step, c, lane);
+    if (wib != 0 || nw == 1) {
+      const int sw_ = nw > 1 ? wib - 1 : 0, snw = nw > 1 ? nw - 1 : 1;
+      if (i + 2 < nblk) cta_stage_rows(C, i + 2, len, W, s.row_bytes, snw, sw_, lane);
+      if (i + 4 < nblk) cta_stage_rv(C, i + 4, start, len, a.ratings, sw_ * 32 + lane, snw * 32);
+    }
+    cp_async_commit();
     bar_sync_named(nthr);
     cta_rows<Store, NV>(X, C.sw, rvb, C.nesh, C.cpow, hcur, hnext, nr, wib * rpg, (wib + 1) * rpg, wib == nw - 1, c,
                         W, s, colkey, i + 1 == nblk ? hrow : nullptr, hkey, lane);

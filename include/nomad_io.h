@@ -151,7 +151,7 @@ typedef struct nomad_synth_spec {
  * Returns NOMAD_ERR_INVALID_ARG for other numbers. */
 int nomad_synth_preset(int32_t workload, nomad_synth_spec* spec);
 
-/* Problem `index` of the batched workload (BASELINE configuration 5), drawn from `seed`:
+/* Problem `index` of the batched workload (4,096 independent problems of uneven shape and rank), drawn from `seed`:
  * m log-uniform in [200, 20,000], n log-uniform in [100, 5,000], density log-uniform in
  * [0.5%, 5%] (90% train / 10% test cells, uniform without replacement), rank k drawn from
  * {16, 32, 64}, planted rank k/4 with N(0, (k/4)^-1/2) factors, values <w*,h*> + N(0, 0.1^2).

@@ -458,7 +458,7 @@ __host__ __device__ inline size_t cta_region_bytes(int kpad, int esz) {
   const size_t rows = static_cast<size_t>(kHStages) * kHB * cta_row_words(kpad, esz) * 4;
   const size_t gram = static_cast<size_t>(kHB) * kGStride * 4;
   const size_t h = (static_cast<size_t>(2) * kpad * 4 + 15) / 16 * 16;
-  return rows + gram + h + 2 * kHB * 4 + static_cast<size_t>(kHRv) * kHB * 8 + 48 * 4;
+  return rows + gram + h + 2 * kHB * 4 + static_cast<size_t>(kHRv) * kHB * 8 + 80 * 4;
 }
 
 struct CtaRegion {
@@ -469,6 +469,7 @@ struct CtaRegion {
   float* nesh;  // kHB: -eta e_t
   int2* rv;     // kHRv x kHB rating indices
   float* cpow;  // kHB + 1: c^k
+  float* cinv;  // kHB: c^-(k+1)
   int sw;
 };
 
@@ -485,6 +486,7 @@ __device__ __forceinline__ CtaRegion cta_region(char* base, int kpad, int esz) {
   C.nesh = C.bsh + kHB;
   C.rv = reinterpret_cast<int2*>(C.nesh + kHB);
   C.cpow = reinterpret_cast<float*>(C.rv + kHRv * kHB);
+  C.cinv = C.cpow + 36;
   return C;
 }
 
@@ -642,11 +644,11 @@ __device__ __forceinline__ void gram_tile(const __nv_bfloat16* X, int sw, int kp
   for (int i = 0; i < 4; ++i) d[i] += d2[i];
 }
 
-// Reduce-scatter of 16 per-lane partials: lane l ends with the warp total of index l % 16.
-__device__ __forceinline__ float reduce_scatter16(float (&v)[16], int lane) {
+// Reduce-scatter of 8 per-lane partials: lane l ends with the warp total of index l % 8.
+__device__ __forceinline__ float reduce_scatter8(float (&v)[8], int lane) {
 #pragma unroll
-  for (int lvl = 0; lvl < 4; ++lvl) {
-    const int half = 8 >> lvl;
+  for (int lvl = 0; lvl < 3; ++lvl) {
+    const int half = 4 >> lvl;
     const bool up = (lane & half) != 0;
 #pragma unroll
     for (int i = 0; i < half; ++i) {
@@ -655,23 +657,25 @@ __device__ __forceinline__ float reduce_scatter16(float (&v)[16], int lane) {
       v[i] = keep + __shfl_xor_sync(kFull, send, half);
     }
   }
-  return v[0] + __shfl_xor_sync(kFull, v[0], 16);
+  const float x = v[0] + __shfl_xor_sync(kFull, v[0], 8);
+  return x + __shfl_xor_sync(kFull, x, 16);
 }
 
-// b_j = <h, x_j> for 16 rows x_j of a block, one warp; lane j ends with b_{j % 16}.
+// b_j = <h, x_j> for 8 rows x_j of a block, one warp; lane j ends with b_{j % 8}.  Four
+// warps cover a block's 32 rows, beside the six warps of its Gram tiles.
 template <typename Store, int NV>
-__device__ __forceinline__ float cta_dots16(const char* X, int sw, const float* h, const Shape& s, int lane) {
+__device__ __forceinline__ float cta_dots8(const char* X, int sw, const float* h, const Shape& s, int lane) {
   using Raw = typename Vec<Store>::Raw;
-  float p[16];
+  float p[8];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) p[j] = 0.f;
+  for (int j = 0; j < 8; ++j) p[j] = 0.f;
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const int v = lane + 32 * q;
     if (v < s.nvec) {
       const float4 hv = reinterpret_cast<const float4*>(h)[v];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
+      for (int j = 0; j < 8; ++j) {
         float w[4];
         nd::unpack(reinterpret_cast<const Raw*>(X + static_cast<size_t>(j) * sw * 4)[v], w);
         p[j] = fmaf(hv.x, w[0], p[j]);
@@ -681,29 +685,39 @@ __device__ __forceinline__ float cta_dots16(const char* X, int sw, const float* 
       }
     }
   }
-  return reduce_scatter16(p, lane);
+  return reduce_scatter8(p, lane);
 }
 
-// The serial part of a block: lane j holds b_j; returns this lane's share of the squared
-// errors and leaves -eta e_t in nesh[t].
-__device__ __forceinline__ float cta_chain(const float* G, const float* bsh, const int2* rvb, float* nesh, int nr,
-                                           float step, float c, int lane) {
-  float bj = bsh[lane];
-  float my_e = 0.f, my_ne = 0.f;
+// The serial part of a block, lane j holding row j.  With b_j = c^t beta_j after step t,
+//   e_t = c^t beta_t - v_t,   beta_j += k_t G_jt  (j > t),   k_t = -eta e_t c^-(t+1),
+// and lane j can form its own k_j as soon as step j - 1 is applied:
+//   k_j = beta_j (-eta / c) + eta v_j c^-(j+1),
+// so a step is one shuffle (k_t from lane t) and two FMAs on the dependent path -- the
+// broadcast k_t updates every lane's beta, and lane t + 1's k is then final.  (Lanes at
+// or below t keep updating values nothing reads again.)  Returns this lane's squared
+// error and leaves -eta e_t in nesh[t] (0 past the block's last rating).
+__device__ __forceinline__ float cta_chain(const float* G, const float* bsh, const int2* rvb, float* nesh,
+                                           const float* cpow, const float* cinv, int nr, float step, float c,
+                                           int lane) {
+  float beta = bsh[lane];
+  const float v = __int_as_float(rvb[lane].y);  // unused past the block's last rating
+  const float a = -step / c;
+  const float bj = step * v * cinv[lane];
+  const float cp = cpow[lane];
+  float k = fmaf(beta, a, bj);  // final for lane 0
+  float my_e = 0.f;
+  // All kHB steps run, without a branch per step: steps past the block's last rating
+  // only change values nothing reads.
 #pragma unroll
   for (int t = 0; t < kHB; ++t) {
-    if (t >= nr) break;
     const float g = G[lane * kGStride + t];  // independent of the chain: loaded ahead
-    const float bt = __shfl_sync(kFull, bj, t);
-    const float e = bt - __int_as_float(rvb[t].y);
-    const float ne = -step * e;
-    my_e = lane == t ? e : my_e;
-    my_ne = lane == t ? ne : my_ne;
-    const float upd = fmaf(ne, g, c * bj);
-    bj = lane > t ? upd : bj;
+    const float kt = __shfl_sync(kFull, k, t);
+    my_e = lane == t ? fmaf(cp, beta, -v) : my_e;  // e_t, from beta before its own update
+    beta = fmaf(kt, g, beta);
+    k = fmaf(beta, a, bj);
   }
-  nesh[lane] = my_ne;  // 0 past the block's last rating
-  return my_e * my_e;
+  nesh[lane] = lane < nr ? -step * my_e : 0.f;
+  return lane < nr ? my_e * my_e : 0.f;
 }
 
 // Rows [t0, t1) of a block (one warp): replay h over the rows before t0, then update
@@ -872,11 +886,15 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
   if (sizeof(Store) == 4 && (kpad & 7) != 0)
     for (int r = tid; r < kHStages * kHB; r += nthr)
       *reinterpret_cast<float4*>(C.rows + static_cast<size_t>(r) * C.sw * 4 + kpad * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (tid == 0) {  // c^k
-    float x = 1.f;
+  if (tid == 0) {  // c^k and c^-(k+1)
+    float x = 1.f, y = 1.f / c, yi = y;
     for (int i = 0; i <= kHB; ++i) {
       C.cpow[i] = x;
       x *= c;
+      if (i < kHB) {
+        C.cinv[i] = yi;
+        yi *= y;
+      }
     }
   }
   cp_async_wait<0>();
@@ -895,8 +913,8 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
     const char* X = C.rows + static_cast<size_t>(i % kHStages) * kHB * C.sw * 4;
     const int2* rvb = C.rv + (i % kHRv) * kHB;
     const int nr = min(kHB, len - i * kHB);
-    // Gram tiles (lower triangle of 16x8 tiles) and the dots with h (two halves)
-    for (int it = wib; it < 8; it += nw) {
+    // Gram tiles (lower triangle of 16x8 tiles) and the dots with h (four quarters)
+    for (int it = wib; it < 10; it += nw) {
       if (it < 6) {
         const int r0 = it < 2 ? 0 : 16;
         const int n0 = it < 2 ? 8 * it : 8 * (it - 2);
@@ -908,9 +926,9 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
         C.G[(r0 + g + 8) * kGStride + n0 + 2 * t] = d[2];
         C.G[(r0 + g + 8) * kGStride + n0 + 2 * t + 1] = d[3];
       } else {
-        const int r0 = 16 * (it - 6);
-        const float bv = cta_dots16<Store, NV>(X + static_cast<size_t>(r0) * C.sw * 4, C.sw, hcur, s, lane);
-        if (lane < 16) C.bsh[r0 + lane] = bv;
+        const int r0 = 8 * (it - 6);
+        const float bv = cta_dots8<Store, NV>(X + static_cast<size_t>(r0) * C.sw * 4, C.sw, hcur, s, lane);
+        if (lane < 8) C.bsh[r0 + lane] = bv;
       }
     }
     bar_sync_named(nthr);
@@ -918,7 +936,7 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
     // and block i + 4's indices (issuing them took 900-2,000 cycles per warp, which at
     // the start of the block delayed the Gram tiles); with one warp, warp 0 issues them
     // after the chain.  Each thread commits one copy group per block either way.
-    if (wib == 0) e2 += cta_chain(C.G, C.bsh, rvb, C.nesh, nr, step, c, lane);
+    if (wib == 0) e2 += cta_chain(C.G, C.bsh, rvb, C.nesh, C.cpow, C.cinv, nr, step, c, lane);
     if (wib != 0 || nw == 1) {
       const int sw_ = nw > 1 ? wib - 1 : 0, snw = nw > 1 ? nw - 1 : 1;
       if (i + 2 < nblk) cta_stage_rows(C, i + 2, len, W, s.row_bytes, snw, sw_, lane);

@@ -429,10 +429,12 @@ __device__ __forceinline__ float visit_long(const SlotHdr* hd, int64_t start, in
 // touches those rows.  The visit runs in blocks of kHB ratings with the chain rewritten
 // exactly, as on the long-visit path:
 //   G = X X^T over the block's (distinct, old) rows X -- tensor cores, 3xTF32 for fp32
-//       rows, exact bf16 products for bf16 rows; b = X h -- one warp;
+//       rows (split into tf32 parts once per block), exact bf16 products for bf16 rows;
+//       b = X h -- four warps;
 //   e_t = b_t - v_t,  b_j <- c b_j - eta e_t G_jt (j > t) -- one warp, lane j holds b_j;
 //   w_t' = c w_t - eta e_t h_t,  h_{t+1} = c h_t - eta e_t w_t -- each warp for its rows,
-//       after replaying the h recurrence over the rows before them.
+//       from h_t = c^t (h_0 + sum_{s<t} k_s w_s), k_s = -eta e_s c^-(s+1), summed over the
+//       rows before them.
 constexpr int kHB = 32;          // ratings per block
 constexpr int kHStages = 3;      // row blocks in shared memory (one in use, two in flight)
 constexpr int kHRv = 8;          // rating-index blocks in shared memory (ring)
@@ -455,18 +457,22 @@ __host__ __device__ inline int cta_row_words(int kpad, int esz) {
   return sw;
 }
 __host__ __device__ inline size_t cta_region_bytes(int kpad, int esz) {
-  const size_t rows = static_cast<size_t>(kHStages) * kHB * cta_row_words(kpad, esz) * 4;
+  // fp32 rows: kHStages staged blocks plus the tf32 high and low parts of one block
+  const size_t rows = static_cast<size_t>(kHStages + (esz == 4 ? 2 : 0)) * kHB * cta_row_words(kpad, esz) * 4;
   const size_t gram = static_cast<size_t>(kHB) * kGStride * 4;
   const size_t h = (static_cast<size_t>(2) * kpad * 4 + 15) / 16 * 16;
-  return rows + gram + h + 2 * kHB * 4 + static_cast<size_t>(kHRv) * kHB * 8 + 80 * 4;
+  return rows + gram + h + 3 * kHB * 4 + static_cast<size_t>(kHRv) * kHB * 8 + 80 * 4;
 }
 
 struct CtaRegion {
   char* rows;   // kHStages x kHB rows of sw words
+  float* xhi;   // fp32 rows: kHB rows of sw words, tf32 high parts of the block the next
+  float* xlo;   //   Gram tiles read; low parts (x - hi rounded to tf32) in xlo
   float* G;     // kHB x kGStride
   float* h;     // 2 x kpad, the held column (fp32) before and after a block
   float* bsh;   // kHB
   float* nesh;  // kHB: -eta e_t
+  float* ksh;   // kHB: k_t = -eta e_t c^-(t+1)
   int2* rv;     // kHRv x kHB rating indices
   float* cpow;  // kHB + 1: c^k
   float* cinv;  // kHB: c^-(k+1)
@@ -478,13 +484,17 @@ __device__ __forceinline__ CtaRegion cta_region(char* base, int kpad, int esz) {
   C.sw = cta_row_words(kpad, esz);
   C.rows = base;
   char* p = base + static_cast<size_t>(kHStages) * kHB * C.sw * 4;
+  C.xhi = reinterpret_cast<float*>(p);
+  C.xlo = C.xhi + kHB * C.sw;
+  if (esz == 4) p += static_cast<size_t>(2) * kHB * C.sw * 4;
   C.G = reinterpret_cast<float*>(p);
   p += static_cast<size_t>(kHB) * kGStride * 4;
   C.h = reinterpret_cast<float*>(p);
   p += (static_cast<size_t>(2) * kpad * 4 + 15) / 16 * 16;
   C.bsh = reinterpret_cast<float*>(p);
   C.nesh = C.bsh + kHB;
-  C.rv = reinterpret_cast<int2*>(C.nesh + kHB);
+  C.ksh = C.nesh + kHB;
+  C.rv = reinterpret_cast<int2*>(C.ksh + kHB);
   C.cpow = reinterpret_cast<float*>(C.rv + kHRv * kHB);
   C.cinv = C.cpow + 36;
   return C;
@@ -581,27 +591,27 @@ __device__ __forceinline__ void ldsm_x2(uint32_t addr, uint32_t (&r)[2]) {
 
 // One 16x8 tile of G = X X^T: rows r0.., columns n0.. (fragment layouts of mma.m16n8k8 /
 // m16n8k16: g = lane / 4 selects the row, t = lane % 4 the k pair or k element).  fp32
-// rows: 3xTF32, three mma per k step (hi*hi into one accumulator, hi*lo + lo*hi into
-// another, summed at the end), so G carries close to fp32 precision like the rest of
-// the fp32 form; b = X h is computed separately in fp32.
-__device__ __forceinline__ void gram_tile(const float* X, int sw, int kpad, int r0, int n0, float (&d)[4], int lane) {
+// rows: 3xTF32 from the block's rows split once into tf32 high and low parts (Xh, Xl),
+// three mma per k step (hi*hi into one accumulator, hi*lo + lo*hi into another, summed at
+// the end), so G carries close to fp32 precision like the rest of the fp32 form; b = X h
+// is computed separately in fp32.
+__device__ __forceinline__ void gram_tile(const float* Xh, const float* Xl, int sw, int kpad, int r0, int n0,
+                                          float (&d)[4], int lane) {
   const int rr = lane & 7, mi = lane >> 3;
   // A: matrices (rows r0.., words k0..), (rows r0+8.., k0..), (r0.., k0+4..), (r0+8.., k0+4..)
-  const uint32_t a_addr = smem_u32(X + (r0 + rr + (mi & 1) * 8) * sw + (mi >> 1) * 4);
+  const uint32_t a_off = 4u * ((r0 + rr + (mi & 1) * 8) * sw + (mi >> 1) * 4);
   // B: matrices (rows n0.., words k0..), (rows n0.., k0+4..) from lanes 0..15
-  const uint32_t b_addr = smem_u32(X + (n0 + rr) * sw + (mi & 1) * 4);
+  const uint32_t b_off = 4u * ((n0 + rr) * sw + (mi & 1) * 4);
+  const uint32_t hs = smem_u32(Xh), ls = smem_u32(Xl);
   float d2[4] = {0.f, 0.f, 0.f, 0.f};  // the cross terms hi*lo + lo*hi
   const int kmma = (kpad + 7) / 8 * 8;  // the row padded with zeros to whole k8 steps
 #pragma unroll 2
   for (int k0 = 0; k0 < kmma; k0 += 8) {
-    uint32_t ar[4], br[2];
-    ldsm_x4(a_addr + 4u * k0, ar);
-    ldsm_x2(b_addr + 4u * k0, br);
     uint32_t ah[4], al[4], bh[2], bl[2];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) split_tf32(__uint_as_float(ar[q]), ah[q], al[q]);
-#pragma unroll
-    for (int q = 0; q < 2; ++q) split_tf32(__uint_as_float(br[q]), bh[q], bl[q]);
+    ldsm_x4(hs + a_off + 4u * k0, ah);
+    ldsm_x4(ls + a_off + 4u * k0, al);
+    ldsm_x2(hs + b_off + 4u * k0, bh);
+    ldsm_x2(ls + b_off + 4u * k0, bl);
     mma_tf32(d2, ah, bl);
     mma_tf32(d2, al, bh);
     mma_tf32(d, ah, bh);
@@ -642,6 +652,17 @@ __device__ __forceinline__ void gram_tile(const __nv_bfloat16* X, int sw, int kp
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) d[i] += d2[i];
+}
+
+// The Gram tile of a block's rows in either form.
+__device__ __forceinline__ void block_gram_tile(const CtaRegion& C, const char* X, const float*, int kpad, int r0,
+                                                int n0, float (&d)[4], int lane) {
+  gram_tile(C.xhi, C.xlo, C.sw, kpad, r0, n0, d, lane);
+  (void)X;
+}
+__device__ __forceinline__ void block_gram_tile(const CtaRegion& C, const char* X, const __nv_bfloat16*, int kpad,
+                                                int r0, int n0, float (&d)[4], int lane) {
+  gram_tile(reinterpret_cast<const __nv_bfloat16*>(X), C.sw, kpad, r0, n0, d, lane);
 }
 
 // Reduce-scatter of 8 per-lane partials: lane l ends with the warp total of index l % 8.
@@ -697,8 +718,8 @@ __device__ __forceinline__ float cta_dots8(const char* X, int sw, const float* h
 // or below t keep updating values nothing reads again.)  Returns this lane's squared
 // error and leaves -eta e_t in nesh[t] (0 past the block's last rating).
 __device__ __forceinline__ float cta_chain(const float* G, const float* bsh, const int2* rvb, float* nesh,
-                                           const float* cpow, const float* cinv, int nr, float step, float c,
-                                           int lane) {
+                                           float* ksh, const float* cpow, const float* cinv, int nr, float step,
+                                           float c, int lane) {
   float beta = bsh[lane];
   const float v = __int_as_float(rvb[lane].y);  // unused past the block's last rating
   const float a = -step / c;
@@ -717,6 +738,7 @@ __device__ __forceinline__ float cta_chain(const float* G, const float* bsh, con
     k = fmaf(beta, a, bj);
   }
   nesh[lane] = lane < nr ? -step * my_e : 0.f;
+  ksh[lane] = lane < nr ? -step * my_e * cinv[lane] : 0.f;
   return lane < nr ? my_e * my_e : 0.f;
 }
 
@@ -724,29 +746,29 @@ __device__ __forceinline__ float cta_chain(const float* G, const float* bsh, con
 // each row and h.  The last warp also leaves h after the block in h_out, or, after the
 // visit's final block, writes it to the column's row `hrow` in HBM.
 template <typename Store, int NV>
-__device__ __forceinline__ void cta_rows(const char* X, int sw, const int2* rvb, const float* nesh, const float* cpow,
+__device__ __forceinline__ void cta_rows(const char* X, int sw, const int2* rvb, const float* nesh, const float* ksh,
+                                         const float* cpow,
                                          const float* h_in, float* h_out, int nr, int t0, int t1, bool last, float c,
                                          void* W, const Shape& s, uint32_t colkey, Store* hrow, uint32_t hkey,
                                          int lane) {
   constexpr int E = Vec<Store>::E;
   using Raw = typename Vec<Store>::Raw;
-  // h_{t0} = c^{t0} h_0 + sum_{s < t0} c^{t0-1-s} (-eta e_s) w_s, two partial sums
+  // h_{t0} = c^{t0} (h_0 + sum_{s < t0} k_s w_s), two partial sums
   const int pre = min(t0, nr);
   float h[NV][E], h2[NV][E];
   {
-    const float cp = cpow[pre];
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
       const int v = lane + 32 * q;
       const float4 x = v < s.nvec ? reinterpret_cast<const float4*>(h_in)[v] : make_float4(0.f, 0.f, 0.f, 0.f);
-      h[q][0] = cp * x.x; h[q][1] = cp * x.y; h[q][2] = cp * x.z; h[q][3] = cp * x.w;
+      h[q][0] = x.x; h[q][1] = x.y; h[q][2] = x.z; h[q][3] = x.w;
 #pragma unroll
       for (int e = 0; e < E; ++e) h2[q][e] = 0.f;
     }
   }
 #pragma unroll 4
   for (int t = 0; t < pre; ++t) {
-    const float coef = cpow[pre - 1 - t] * nesh[t];
+    const float coef = ksh[t];
     const Raw* row = reinterpret_cast<const Raw*>(X + static_cast<size_t>(t) * sw * 4);
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
@@ -762,10 +784,13 @@ __device__ __forceinline__ void cta_rows(const char* X, int sw, const int2* rvb,
       }
     }
   }
+  {
+    const float cp = cpow[pre];
 #pragma unroll
-  for (int q = 0; q < NV; ++q)
+    for (int q = 0; q < NV; ++q)
 #pragma unroll
-    for (int e = 0; e < E; ++e) h[q][e] += h2[q][e];
+      for (int e = 0; e < E; ++e) h[q][e] = cp * (h[q][e] + h2[q][e]);
+  }
   const int end = min(t1, nr);
   for (int t = t0; t < end; ++t) {
     const float ne = nesh[t];
@@ -852,6 +877,30 @@ __device__ __forceinline__ void cta_stage_rv(const CtaRegion& C, int b, int64_t 
   }
 }
 
+// fp32 rows: the tf32 high and low parts of block b's rows for the Gram tiles, split by
+// the threads that staged them -- each thread its own chunks (rows wib, wib + nw, ... and
+// 16-byte chunks lane, lane + 32, ... of each, as cta_stage_rows copies them), once its
+// copies have landed, so no other thread's copies need to be waited for.
+template <typename Store>
+__device__ __forceinline__ void cta_split_rows(const CtaRegion& C, int b, int len, int row_bytes, int nw, int wib,
+                                               int lane) {
+  if (sizeof(Store) != 4) return;
+  const int nrb = min(kHB, len - b * kHB);
+  const float* X = reinterpret_cast<const float*>(C.rows + static_cast<size_t>(b % kHStages) * kHB * C.sw * 4);
+  const int cpr = row_bytes / 16;
+  for (int r = wib; r < nrb; r += nw)
+    for (int k = lane; k < cpr; k += 32) {
+      const float4 x = reinterpret_cast<const float4*>(X + r * C.sw)[k];
+      uint4 h, l;
+      split_tf32(x.x, h.x, l.x);
+      split_tf32(x.y, h.y, l.y);
+      split_tf32(x.z, h.z, l.z);
+      split_tf32(x.w, h.w, l.w);
+      reinterpret_cast<uint4*>(C.xhi + r * C.sw)[k] = h;
+      reinterpret_cast<uint4*>(C.xlo + r * C.sw)[k] = l;
+    }
+}
+
 // One visit of priority token `tok` by the block's nw live warps (all of them call it).
 // The last warp writes the column back; warp 0 returns the squared errors.  The shared
 // region is free again when this returns (the warps' long-visit rings alias it).
@@ -882,9 +931,10 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
     nd::load_vec_cg<Store>(hrow, v, x);
     reinterpret_cast<float4*>(C.h)[v] = make_float4(x[0], x[1], x[2], x[3]);
   }
-  // zero the columns past an fp32 row that the last k8 tile reads
+  // zero the columns past an fp32 row that the last k8 tile reads (staged rows and the
+  // tf32 parts, which follow them)
   if (sizeof(Store) == 4 && (kpad & 7) != 0)
-    for (int r = tid; r < kHStages * kHB; r += nthr)
+    for (int r = tid; r < (kHStages + 2) * kHB; r += nthr)
       *reinterpret_cast<float4*>(C.rows + static_cast<size_t>(r) * C.sw * 4 + kpad * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
   if (tid == 0) {  // c^k and c^-(k+1)
     float x = 1.f, y = 1.f / c, yi = y;
@@ -903,6 +953,8 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
   cp_async_commit();
   if (nblk > 1) cta_stage_rows(C, 1, len, W, s.row_bytes, nw, wib, lane);
   cp_async_commit();
+  cp_async_wait<1>();  // this thread's copies of block 0's rows have landed
+  cta_split_rows<Store>(C, 0, len, s.row_bytes, nw, wib, lane);
   float e2 = 0.f;
   const int rpg = (kHB + nw - 1) / nw;
   for (int i = 0; i < nblk; ++i) {
@@ -919,7 +971,7 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
         const int r0 = it < 2 ? 0 : 16;
         const int n0 = it < 2 ? 8 * it : 8 * (it - 2);
         float d[4] = {0.f, 0.f, 0.f, 0.f};
-        gram_tile(reinterpret_cast<const Store*>(X), C.sw, kpad, r0, n0, d, lane);
+        block_gram_tile(C, X, static_cast<const Store*>(nullptr), kpad, r0, n0, d, lane);
         const int g = lane >> 2, t = lane & 3;
         C.G[(r0 + g) * kGStride + n0 + 2 * t] = d[0];
         C.G[(r0 + g) * kGStride + n0 + 2 * t + 1] = d[1];
@@ -936,7 +988,17 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
     // and block i + 4's indices (issuing them took 900-2,000 cycles per warp, which at
     // the start of the block delayed the Gram tiles); with one warp, warp 0 issues them
     // after the chain.  Each thread commits one copy group per block either way.
-    if (wib == 0) e2 += cta_chain(C.G, C.bsh, rvb, C.nesh, C.cpow, C.cinv, nr, step, c, lane);
+    if (wib == 0) e2 += cta_chain(C.G, C.bsh, rvb, C.nesh, C.ksh, C.cpow, C.cinv, nr, step, c, lane);
+    // fp32 rows: the tf32 parts of block i + 1, split by the threads that staged it (every
+    // warp for block 1, the copying warps after it; warp 0 after its chain)
+    if (sizeof(Store) == 4 && i + 1 < nblk) {
+      const bool all = i == 0;
+      if (all || wib != 0 || nw == 1) {
+        cp_async_wait<0>();
+        cta_split_rows<Store>(C, i + 1, len, s.row_bytes, all ? nw : (nw > 1 ? nw - 1 : 1),
+                              all ? wib : (nw > 1 ? wib - 1 : 0), lane);
+      }
+    }
     if (wib != 0 || nw == 1) {
       const int sw_ = nw > 1 ? wib - 1 : 0, snw = nw > 1 ? nw - 1 : 1;
       if (i + 2 < nblk) cta_stage_rows(C, i + 2, len, W, s.row_bytes, snw, sw_, lane);
@@ -944,7 +1006,7 @@ __device__ __forceinline__ void cta_visit(int tok, const nomad::AsyncArgs& a, co
     }
     cp_async_commit();
     bar_sync_named(nthr);
-    cta_rows<Store, NV>(X, C.sw, rvb, C.nesh, C.cpow, hcur, hnext, nr, wib * rpg, (wib + 1) * rpg, wib == nw - 1, c,
+    cta_rows<Store, NV>(X, C.sw, rvb, C.nesh, C.ksh, C.cpow, hcur, hnext, nr, wib * rpg, (wib + 1) * rpg, wib == nw - 1, c,
                         W, s, colkey, i + 1 == nblk ? hrow : nullptr, hkey, lane);
   }
   cp_async_wait<0>();

@@ -716,7 +716,8 @@ __device__ __forceinline__ float cta_dots8(const char* X, int sw, const float* h
 // so a step is one shuffle (k_t from lane t) and two FMAs on the dependent path -- the
 // broadcast k_t updates every lane's beta, and lane t + 1's k is then final.  (Lanes at
 // or below t keep updating values nothing reads again.)  Returns this lane's squared
-// error and leaves -eta e_t in nesh[t] (0 past the block's last rating).
+// error and leaves -eta e_t in nesh[t] and k_t = -eta e_t c^-(t+1) in ksh[t] (both 0 past
+// the block's last rating).
 __device__ __forceinline__ float cta_chain(const float* G, const float* bsh, const int2* rvb, float* nesh,
                                            float* ksh, const float* cpow, const float* cinv, int nr, float step,
                                            float c, int lane) {
@@ -742,9 +743,9 @@ __device__ __forceinline__ float cta_chain(const float* G, const float* bsh, con
   return lane < nr ? my_e * my_e : 0.f;
 }
 
-// Rows [t0, t1) of a block (one warp): replay h over the rows before t0, then update
-// each row and h.  The last warp also leaves h after the block in h_out, or, after the
-// visit's final block, writes it to the column's row `hrow` in HBM.
+// Rows [t0, t1) of a block (one warp): form h at row t0 from the rows before it, then
+// update each row and h.  The last warp also leaves h after the block in h_out, or, after
+// the visit's final block, writes it to the column's row `hrow` in HBM.
 template <typename Store, int NV>
 __device__ __forceinline__ void cta_rows(const char* X, int sw, const int2* rvb, const float* nesh, const float* ksh,
                                          const float* cpow,

@@ -267,10 +267,15 @@ def e2e_run(ng, train, test, K, device, args):
               workers=args.workers, warps_per_block=args.wpb, blocks_per_sm=args.bps)
     t0 = time.perf_counter()
     nm = ng.Nomad(train, test, **kw)
+    t1 = time.perf_counter()
     upd = 0
+    dev_ms = 0.0
     for _ in range(K):
-        upd += nm.epoch(1)["updates"]  # the epoch's stats carry its online training loss
+        st = nm.epoch(1)               # the epoch's stats carry its online training loss
+        upd += st["updates"]
+        dev_ms += st["device_ms"]
         nm.rmse(train=False)           # the step's metric: test RMSE
+    t2 = time.perf_counter()
     nm.rmse()                          # the job's result: both RMSEs and the factors
     nm.factors()
     info = nm.info()
@@ -279,7 +284,8 @@ def e2e_run(ng, train, test, K, device, args):
     return {"value": upd / dt, "unit": UNIT,
             "h2d_bytes_per_step": int(info["h2d_bytes"] // max(K, 1)),
             "d2h_bytes_per_step": int(info["d2h_bytes"] // max(K, 1)),
-            "seconds": dt}
+            "seconds": dt, "setup_s": t1 - t0, "steps_s": t2 - t1, "steps_device_s": dev_ms / 1e3,
+            "result_s": dt - (t2 - t0)}
 
 
 def cpu_baseline(train, seconds):

@@ -25,6 +25,11 @@ int host_threads(int requested = 0);
 // Run fn(t, lo, hi) on `threads` contiguous chunks of [0, count).
 void parallel_chunks(int64_t count, int threads,
                      const std::function<void(int, int64_t, int64_t)>& fn);
+// Writes a zero into every page of an output buffer that is about to be filled by a
+// device-to-host copy, on `threads` threads: a copy into pages that are not yet mapped
+// takes its page faults one after another inside the copy (~0.3 GB/s on the GB300's host),
+// touched pages take the copy at full speed.
+void prefault(void* p, size_t bytes, int threads);
 // Chunks of `grain` items handed to `threads` threads on demand (for uneven items);
 // fn(thread, lo, hi) as for parallel_chunks.
 void parallel_dynamic(int64_t count, int64_t grain, int threads,

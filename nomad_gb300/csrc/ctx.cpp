@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -168,6 +169,12 @@ int get_factor(nomad_gpu_ctx* c, const void* src, float* dst, int64_t rows) {
   const int64_t chunk_rows = std::max<int64_t>(1, (int64_t(16) << 20) / std::max(f.dim, 1));
   float* stage = nullptr;
   CK(cudaMalloc(&stage, std::max<int64_t>(1, std::min(rows, chunk_rows)) * f.dim * sizeof(float)));
+  {  // pageable host memory only: touch its pages ahead of the copies
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, dst) == cudaSuccess && pa.type == cudaMemoryTypeUnregistered)
+      nomad::prefault(dst, static_cast<size_t>(rows) * f.dim * sizeof(float), nomad::host_threads());
+    cudaGetLastError();
+  }
   const size_t esz = f.bf16 ? 2 : 4;
   int rc = NOMAD_OK;
   for (int64_t r0 = 0; r0 < rows && rc == NOMAD_OK; r0 += chunk_rows) {
@@ -193,6 +200,50 @@ int upload_csc(nomad_gpu_ctx* c, const nomad::Csc& csc, int2** ratings, int64_t*
   CK(cudaMemsetAsync(*ratings + n, 0, 2 * sizeof(int2), c->stream));
   if (n) CK(cudaMemcpyAsync(*ratings, csc.ratings.data(), n * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
   c->h2d_bytes += static_cast<int64_t>(n * sizeof(int2));
+  return NOMAD_OK;
+}
+
+// A rating set whose CSC is built on the device: row-major (the order the sort keeps),
+// and few enough ratings for 32-bit sort indices.
+bool device_csc_ok(const nomad_gpu_matrix& A) {
+  return A.row_counts && A.nnz > 0 && A.nnz <= INT_MAX && A.cols && (A.vals_f64 || A.vals_f32);
+}
+
+// The CSC of a checked row-major set built on the device (csc_device.cu) into the context's
+// buffers; its col_ptr (and with `with_ratings` the row of every rating, for the layout
+// builds) copied to `host` when that is given.
+int device_csc_set(nomad_gpu_ctx* c, const nomad_gpu_matrix& A, int32_t m, int32_t n, int2** ratings, int64_t** ptr,
+                   nomad::Csc* host, bool with_ratings) {
+  const size_t nnz = static_cast<size_t>(A.nnz);
+  // two spare entries: 16-byte-rounded prefetches of a run may reach 8 bytes past its end
+  RC(dalloc(c, ratings, nnz + 2));
+  RC(dalloc(c, ptr, static_cast<size_t>(n) + 1));
+  CK(cudaMemsetAsync(*ratings + nnz, 0, 2 * sizeof(int2), c->stream));
+  int32_t dup = -1;
+  int64_t bad = -1;
+  const cudaError_t e = nomad::device_csc(A.nnz, m, n, A.row_counts, A.cols, A.vals_f64, A.vals_f32, *ratings, *ptr,
+                                          &bad, &dup, &c->h2d_bytes, c->stream);
+  if (bad >= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "column index %d out of range [0, %d)", A.cols[bad], n);
+  CK(e);
+  if (dup >= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "repeated (row, column) cell in column %d", dup);
+  nomad::InitTrace trace;
+  if (host) {
+    host->m = m;
+    host->n = n;
+    host->col_ptr.resize(static_cast<size_t>(n) + 1);
+    host->row_nnz.assign(A.row_counts, A.row_counts + m);
+    CK(cudaMemcpyAsync(host->col_ptr.data(), *ptr, (static_cast<size_t>(n) + 1) * sizeof(int64_t),
+                       cudaMemcpyDeviceToHost, c->stream));
+    c->d2h_bytes += static_cast<int64_t>((static_cast<size_t>(n) + 1) * sizeof(int64_t));
+    CK(cudaStreamSynchronize(c->stream));
+    if (with_ratings) {  // the rows alone: all the layout builds read
+      host->rows.resize(nnz);
+      nomad::prefault(host->rows.data(), nnz * sizeof(int32_t), nomad::host_threads());
+      CK(nomad::device_csc_rows(*ratings, A.nnz, host->rows.data(), c->stream));
+      c->d2h_bytes += static_cast<int64_t>(nnz * sizeof(int32_t));
+    }
+    trace.mark("  csc: copies out");
+  }
   return NOMAD_OK;
 }
 
@@ -265,10 +316,16 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   if (host_w) tw = std::thread([&] { rc_w = nomad_reference_init(f.m, 0, f.dim, p.seed, p.init_parts, Wh.data(), nullptr); });
   if (host_h) th = std::thread([&] { rc_h = nomad_reference_init(0, f.n, f.dim, p.seed, p.init_parts, nullptr, Hh.data()); });
   // ---- rating sets ---------------------------------------------------------------
+  // Row-major sets are sorted into CSC order on the device (their row counts are checked
+  // here first, their column indices on the device before the sort); COO input and sets
+  // past INT_MAX ratings are sorted on the host.
   nomad::Csc train, test;
-  RC(nomad::build_csc(prob->train, f.m, f.n, train, threads));
-  RC(nomad::build_csc(prob->test, f.m, f.n, test, threads));
-  trace.mark("CSC build (factor init beside it)");
+  const bool dev_train = device_csc_ok(prob->train), dev_test = device_csc_ok(prob->test);
+  if (dev_train) RC(nomad::check_rating_set(prob->train, f.m, f.n, threads, false));
+  else RC(nomad::build_csc(prob->train, f.m, f.n, train, threads));
+  if (dev_test) RC(nomad::check_rating_set(prob->test, f.m, f.n, threads, false));
+  else RC(nomad::build_csc(prob->test, f.m, f.n, test, threads));
+  trace.mark("CSC checks / host builds (factor init beside it)");
   if (tw.joinable()) tw.join();
   if (th.joinable()) th.join();
   if (rc_w != NOMAD_OK || rc_h != NOMAD_OK) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "reference init of the factors failed");
@@ -283,13 +340,18 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
     RC(put_factor(c, f.H, Hh.data(), f.n));
   }
   trace.mark("factors (init wait + upload)", c->stream);
-  c->nnz_train = train.nnz();
-  c->nnz_test = test.nnz();
-  RC(upload_csc(c, train, &c->train, &c->train_ptr));
-  RC(upload_csc(c, test, &c->test, &c->test_ptr));
+  c->nnz_train = prob->train.nnz;
+  c->nnz_test = prob->test.nnz;
+  // the host layout build of the asynchronous modes reads the training CSC, so there it
+  // comes back from the device (else only its column offsets)
+  if (dev_train)
+    RC(device_csc_set(c, prob->train, f.m, f.n, &c->train, &c->train_ptr, &train, p.mode == NOMAD_MODE_ASYNC));
+  else RC(upload_csc(c, train, &c->train, &c->train_ptr));
+  if (dev_test) RC(device_csc_set(c, prob->test, f.m, f.n, &c->test, &c->test_ptr, nullptr, false));
+  else RC(upload_csc(c, test, &c->test, &c->test_ptr));
   for (int32_t j = 0; j < f.n; ++j)
     c->max_column = std::max<int64_t>(c->max_column, train.col_ptr[j + 1] - train.col_ptr[j]);
-  trace.mark("CSC upload", c->stream);
+  trace.mark("CSC on the device", c->stream);
 
   // ---- mode-specific layout --------------------------------------------------------
   if (p.mode == NOMAD_MODE_ASYNC) {

@@ -10,6 +10,8 @@
 #include <limits>
 #include <random>
 
+#include <unistd.h>
+
 #include "common.h"
 
 namespace nomad {
@@ -54,6 +56,21 @@ void parallel_dynamic(int64_t count, int64_t grain, int threads,
   pool.reserve(threads);
   for (int t = 0; t < threads; ++t) pool.emplace_back(run, t);
   for (auto& th : pool) th.join();
+}
+
+void prefault(void* p, size_t bytes, int threads) {
+  if (!p || bytes == 0) return;
+  const long ps = sysconf(_SC_PAGESIZE);
+  const size_t page = ps > 0 ? static_cast<size_t>(ps) : 4096;
+  char* b = static_cast<char*>(p);
+  const int64_t pages = static_cast<int64_t>((bytes + page - 1) / page);
+  const int t = static_cast<int>(std::min<int64_t>(threads, std::max<int64_t>(1, pages / 64)));
+  parallel_chunks(pages, t, [&](int, int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      const size_t at = std::min(static_cast<size_t>(i) * page, bytes - 1);
+      reinterpret_cast<volatile char*>(b)[at] = 0;
+    }
+  });
 }
 
 void parallel_chunks(int64_t count, int threads,

@@ -106,6 +106,11 @@ float step_size_f32(double lrate, double drate, int32_t cnt) {
   return static_cast<float>(learn_rate * 1.5 / (1.0 + decay_rate * std::pow(cnt + 1, 1.5)));
 }
 
+int check_rating_set(const nomad_gpu_matrix& A, int32_t m, int32_t n, int threads, bool check_cols) {
+  RowMajor R;
+  return to_row_major(A, m, n, R, threads, check_cols);
+}
+
 int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int threads) {
   RowMajor R;
   int rc = to_row_major(A, m, n, R, threads, false);
@@ -198,7 +203,7 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
       parallel_chunks(nnz, nt, [&](int t, int64_t lo, int64_t hi) {
         std::vector<int32_t>& h = part[static_cast<size_t>(t)];
         h.assign(static_cast<size_t>(m), 0);
-        for (int64_t o = lo; o < hi; ++o) ++h[csc.ratings[o].row];
+        for (int64_t o = lo; o < hi; ++o) ++h[csc.row(o)];
       });
       counted.assign(static_cast<size_t>(m), 0);
       parallel_chunks(m, nt, [&](int, int64_t lo, int64_t hi) {
@@ -245,7 +250,7 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
       int64_t c = 0;
       int32_t w = -1, wend = 0;
       for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
-        const int32_t r = csc.ratings[o].row;
+        const int32_t r = csc.row(o);
         if (w < 0 || r >= wend) {
           std::tie(w, wend) = owner_of(r, pri);
           ++c;
@@ -266,7 +271,7 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
       int64_t c = -1;
       int32_t w = -1, wend = 0;
       for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
-        const int32_t r = csc.ratings[o].row;
+        const int32_t r = csc.row(o);
         if (w < 0 || r >= wend) {
           std::tie(w, wend) = owner_of(r, pri);
           ++c;

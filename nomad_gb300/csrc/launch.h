@@ -146,6 +146,18 @@ cudaError_t launch_async2(const AsyncArgs& a, cudaStream_t s);
 cudaError_t launch_seed_queues(const AsyncArgs& a, const int4* first_mail, const int2* first_q,
                                const int* counts, int n, int ep, cudaStream_t s);
 cudaError_t launch_drain_queues(const AsyncArgs& a, cudaStream_t s);
+// The CSC of a row-major rating set (row counts, column indices, fp64 or fp32 values, all
+// host arrays; the row counts already checked to add up to nnz) built on the device by a
+// stable radix sort of the entries by column, so rows stay ascending inside a column:
+// ratings {row, value bits} (nnz entries) and col_ptr (n + 1), both caller-allocated.
+// A column index outside [0, n) stops it before the sort with cudaErrorInvalidValue and
+// its entry in *bad_col (else -1); *dup_col is the first column with a repeated (row,
+// column) cell, else -1; *h2d_bytes grows by the bytes copied in.  1 <= nnz <= INT_MAX.
+cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_counts, const int32_t* cols,
+                       const double* v64, const float* v32, int2* ratings, int64_t* col_ptr, int64_t* bad_col,
+                       int32_t* dup_col, int64_t* h2d_bytes, cudaStream_t s);
+// The rows of a device CSC's ratings (nnz entries) copied to host memory.
+cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s);
 cudaError_t launch_build_segx(const int4* segs, const int2* ratings, int64_t nseg, int4* segx, cudaStream_t s);
 cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int cta_heavy, int* blocks_per_sm);
 cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);

@@ -67,7 +67,11 @@ struct Csc {
   std::vector<int64_t> col_ptr;  // [n+1]
   std::vector<Rating, NoInitAllocator<Rating>> ratings;  // [nnz]
   std::vector<int32_t> row_nnz;  // [m] ratings per row (from the row-major input)
+  // [nnz] the rows alone, in place of `ratings`, for a CSC kept on the device whose host
+  // copy only feeds the layout builds
+  std::vector<int32_t, NoInitAllocator<int32_t>> rows;
   int64_t nnz() const { return col_ptr.empty() ? 0 : col_ptr.back(); }
+  int32_t row(int64_t o) const { return rows.empty() ? ratings[o].row : rows[o]; }
 };
 
 // A token visit: the ratings of one column owned by one worker.  16 bytes, read by
@@ -106,6 +110,11 @@ struct DsgdLayout {
   std::vector<int64_t> blk_ptr;  // [innerB * col_blocks + 1]
   std::vector<int32_t> rates;    // 4 ints per entry: row, col, float bits, 0
 };
+
+// The argument checks of build_csc that need no sort (array presence, row counts adding
+// up to nnz, with check_cols column indices in range), for a CSC built elsewhere
+// (csc_device.cu).
+int check_rating_set(const nomad_gpu_matrix& A, int32_t m, int32_t n, int threads, bool check_cols);
 
 // Build the CSC of a rating set given in the row-major file layout or as COO.
 // Fails on out-of-range indices and on repeated (row, column) cells.

@@ -241,6 +241,31 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     const int32_t g = w / group;
     return std::make_pair(g, L.row_start[std::min<int64_t>(static_cast<int64_t>(g + 1) * group, P)]);
   };
+  // End of the run that starts at rating o of a column ending at e: the first rating past
+  // o whose row is at least wend.  Rows ascend inside a column: a short scan covers the
+  // common short run, then a galloping search takes a long one in O(log len).
+  auto run_end = [&](int64_t o, int64_t e, int32_t wend) {
+    int64_t lo = o + 1;
+    for (int i = 0; i < 8; ++i, ++lo)
+      if (lo >= e || csc.row(lo) >= wend) return lo;
+    int64_t step = 1;
+    while (lo < e && csc.row(lo) < wend) {
+      const int64_t hi = std::min(e, lo + step);
+      if (hi < e && csc.row(hi) < wend) {
+        lo = hi + 1;
+        step <<= 1;
+        continue;
+      }
+      int64_t a = lo, b = hi;  // first index in [a, b) with row >= wend (b if none)
+      while (a < b) {
+        const int64_t mid = a + (b - a) / 2;
+        if (csc.row(mid) < wend) a = mid + 1;
+        else b = mid;
+      }
+      return a;
+    }
+    return lo;
+  };
   // columns are uneven (a Zipf column holds ~5% of all ratings): hand them out in small
   // chunks on demand
   std::vector<int64_t> nseg(n, 0);
@@ -248,14 +273,8 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     for (int64_t j = lo; j < hi; ++j) {
       const bool pri = is_priority(j);
       int64_t c = 0;
-      int32_t w = -1, wend = 0;
-      for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
-        const int32_t r = csc.row(o);
-        if (w < 0 || r >= wend) {
-          std::tie(w, wend) = owner_of(r, pri);
-          ++c;
-        }
-      }
+      const int64_t e = csc.col_ptr[j + 1];
+      for (int64_t o = csc.col_ptr[j]; o < e; ++c) o = run_end(o, e, owner_of(csc.row(o), pri).second);
       nseg[j] = c;
     }
   });
@@ -268,16 +287,13 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     for (int64_t j = lo; j < hi; ++j) {
       Segment* s = L.segs.data() + L.vl_ptr[j];
       const bool pri = is_priority(j);
-      int64_t c = -1;
-      int32_t w = -1, wend = 0;
-      for (int64_t o = csc.col_ptr[j]; o < csc.col_ptr[j + 1]; ++o) {
-        const int32_t r = csc.row(o);
-        if (w < 0 || r >= wend) {
-          std::tie(w, wend) = owner_of(r, pri);
-          ++c;
-          s[c] = Segment{o, 0, w};
-        }
-        s[c].len++;
+      const int64_t e = csc.col_ptr[j + 1];
+      int64_t c = 0;
+      for (int64_t o = csc.col_ptr[j]; o < e; ++c) {
+        const auto own = owner_of(csc.row(o), pri);
+        const int64_t next = run_end(o, e, own.second);
+        s[c] = Segment{o, static_cast<int32_t>(next - o), own.first};
+        o = next;
       }
       const int64_t k = nseg[j];
       for (int64_t i = 0; i < k; ++i) maxseg[t] = std::max<int64_t>(maxseg[t], s[i].len);

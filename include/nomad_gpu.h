@@ -97,7 +97,10 @@ typedef struct nomad_gpu_params {
                              progress and the call returns NOMAD_ERR_TIMEOUT (2000)  */
   int32_t debug_flags; /* test hooks; bit 0 = enqueue no tokens (forces a timeout);   *
                         * bit 1 = one worker per thread block never joins a block     *
-                        * visit (the others' join wait runs out: a timeout)           */
+                        * visit (the others' join wait runs out: a timeout);          *
+                        * bit 2 = ASYNC: build the visit lists on the host as well as *
+                        * on the device and refuse with NOMAD_ERR_BOUNDS if they      *
+                        * differ                                                      */
   int32_t long_visit;  /* ASYNC: visits with at least this many ratings run the blocked
                           (7-rating) path with TMA-staged rows; 0 = default 14        */
   int32_t priority_permille; /* ASYNC: columns with at least this many permille of the

@@ -22,7 +22,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["kernels_async.cu", "kernels_sgd.cu", "kernels_eval.cu", "csc_device.cu"]
+CU_SOURCES = ["kernels_async.cu", "kernels_sgd.cu", "kernels_eval.cu", "csc_device.cu", "layout_device.cu"]
 CPP_SOURCES = ["ctx.cpp", "batch.cpp", "host_layout.cpp", "host_io.cpp", "host_synth.cpp"]
 CLI_SOURCES = ["nomad_main.cpp"]
 

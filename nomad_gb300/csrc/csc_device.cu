@@ -8,7 +8,10 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstring>
+#include <mutex>
 
+#include "common.h"
 #include "launch.h"
 #include "trace.h"
 
@@ -59,9 +62,49 @@ __global__ void rows_kernel(const int2* ratings, int64_t nnz, int32_t* rows) {
   if (i < nnz) rows[i] = ratings[i].x;
 }
 
+// Two pinned staging buffers for uploads from pageable memory, kept for the life of the
+// process and used under a lock.
+constexpr size_t kStageBytes = size_t{32} << 20;
+std::mutex g_stage_mu;
+char* g_stage[2] = {nullptr, nullptr};
+
 }  // namespace
 
 namespace nomad {
+
+cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(g_stage_mu);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+    if (!g_stage[i]) e = cudaHostAlloc(reinterpret_cast<void**>(&g_stage[i]), kStageBytes, cudaHostAllocPortable);
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+  const int threads = host_threads();
+  bool used[2] = {false, false};
+  for (size_t off = 0, k = 0; off < bytes && e == cudaSuccess; off += kStageBytes, k ^= 1) {
+    const size_t n = std::min(kStageBytes, bytes - off);
+    if (used[k]) e = cudaEventSynchronize(done[k]);  // the copy out of this buffer is done
+    if (e != cudaSuccess) break;
+    const char* from = static_cast<const char*>(src) + off;
+    char* to = g_stage[k];
+    const int64_t pieces = static_cast<int64_t>((n + (size_t{1} << 20) - 1) >> 20);
+    parallel_chunks(pieces, threads, [&](int, int64_t lo, int64_t hi) {
+      const size_t a = static_cast<size_t>(lo) << 20, b = std::min(n, static_cast<size_t>(hi) << 20);
+      std::memcpy(to + a, from + a, b - a);
+    });
+    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, to, n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(done[k], s);
+    used[k] = true;
+  }
+  // the buffers are reused by the next upload: its copies into them wait for these
+  for (int i = 0; i < 2; ++i)
+    if (done[i]) {
+      if (used[i] && e == cudaSuccess) e = cudaEventSynchronize(done[i]);
+      cudaEventDestroy(done[i]);
+    }
+  return e;
+}
 
 cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s) {
   if (nnz <= 0 || nnz > INT_MAX) return cudaErrorInvalidValue;
@@ -116,11 +159,11 @@ cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_cou
   alloc(&vals, vbytes);
   alloc(&tmp, tmp_bytes);
   if (trace.on && e == cudaSuccess) trace.mark("  csc: allocations", s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(keys_in, cols, static_cast<size_t>(nnz) * 4, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(rc, row_counts, static_cast<size_t>(m) * 4, cudaMemcpyHostToDevice, s);
+  // the caller's arrays are pageable memory of any mapping: staged through pinned buffers
+  if (e == cudaSuccess) e = upload_staged(keys_in, cols, static_cast<size_t>(nnz) * 4, s);
+  if (e == cudaSuccess) e = upload_staged(rc, row_counts, static_cast<size_t>(m) * 4, s);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(vals, v64 ? static_cast<const void*>(v64) : static_cast<const void*>(v32), vbytes,
-                        cudaMemcpyHostToDevice, s);
+    e = upload_staged(vals, v64 ? static_cast<const void*>(v64) : static_cast<const void*>(v32), vbytes, s);
   if (e == cudaSuccess) {
     *h2d_bytes += static_cast<int64_t>(nnz) * 4 + static_cast<int64_t>(m) * 4 + static_cast<int64_t>(vbytes);
     const int dup_none = INT_MAX;

@@ -257,6 +257,35 @@ int reset_tokens(nomad_gpu_ctx* c) {
   return NOMAD_OK;
 }
 
+// Test hook (debug bit 2): the host build of the same layout, compared with the device
+// build field by field; NOMAD_ERR_BOUNDS names the first field that differs.
+int check_device_layout(nomad_gpu_ctx* c, const nomad::Csc& train, const nomad_gpu_params& p, int64_t pri_min,
+                        int32_t group, const nomad::AsyncLayout& L, int threads) {
+  nomad::AsyncLayout H;
+  RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, group, !p.exact, H, threads));
+  std::vector<nomad::Segment> segs(static_cast<size_t>(c->n_segments));
+  CK(cudaMemcpy(segs.data(), c->segs, segs.size() * sizeof(nomad::Segment), cudaMemcpyDeviceToHost));
+  auto same_segs = [&] {
+    if (segs.size() != H.segs.size()) return false;
+    for (size_t i = 0; i < segs.size(); ++i)
+      if (segs[i].start != H.segs[i].start || segs[i].len != H.segs[i].len || segs[i].worker != H.segs[i].worker)
+        return false;
+    return true;
+  };
+  const char* bad = nullptr;
+  if (L.row_start != H.row_start) bad = "row blocks";
+  else if (!same_segs()) bad = "visits";
+  else if (L.vl_ptr != H.vl_ptr) bad = "visit offsets";
+  else if (L.desc0 != H.desc0 || L.first_mail != H.first_mail) bad = "first visits";
+  else if (L.first_q != H.first_q || L.q_count != H.q_count || L.qnext0 != H.qnext0 || L.qtail0 != H.qtail0)
+    bad = "initial queues";
+  else if (L.n_active != H.n_active || L.n_priority != H.n_priority || L.max_segment != H.max_segment ||
+           L.max_column != H.max_column)
+    bad = "counts";
+  if (bad) NOMAD_FAIL(NOMAD_ERR_BOUNDS, "device layout differs from the host layout: %s", bad);
+  return NOMAD_OK;
+}
+
 int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   const nomad_gpu_params& p = c->prm;
   const int threads = nomad::host_threads();
@@ -321,6 +350,8 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   // past INT_MAX ratings are sorted on the host.
   nomad::Csc train, test;
   const bool dev_train = device_csc_ok(prob->train), dev_test = device_csc_ok(prob->test);
+  // the asynchronous modes' visit lists follow the training CSC onto the device
+  const bool dev_layout = dev_train && p.mode == NOMAD_MODE_ASYNC;
   if (dev_train) RC(nomad::check_rating_set(prob->train, f.m, f.n, threads, false));
   else RC(nomad::build_csc(prob->train, f.m, f.n, train, threads));
   if (dev_test) RC(nomad::check_rating_set(prob->test, f.m, f.n, threads, false));
@@ -342,10 +373,11 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
   trace.mark("factors (init wait + upload)", c->stream);
   c->nnz_train = prob->train.nnz;
   c->nnz_test = prob->test.nnz;
-  // the host layout build of the asynchronous modes reads the training CSC, so there it
-  // comes back from the device (else only its column offsets)
+  // a host layout build of the asynchronous modes reads the training CSC's rows, so then
+  // they come back from the device (else only its column offsets)
   if (dev_train)
-    RC(device_csc_set(c, prob->train, f.m, f.n, &c->train, &c->train_ptr, &train, p.mode == NOMAD_MODE_ASYNC));
+    RC(device_csc_set(c, prob->train, f.m, f.n, &c->train, &c->train_ptr, &train,
+                      p.mode == NOMAD_MODE_ASYNC && (!dev_layout || (p.debug_flags & 4))));
   else RC(upload_csc(c, train, &c->train, &c->train_ptr));
   if (dev_test) RC(device_csc_set(c, prob->test, f.m, f.n, &c->test, &c->test_ptr, nullptr, false));
   else RC(upload_csc(c, test, &c->test, &c->test_ptr));
@@ -398,13 +430,36 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       pri_min = std::max<int64_t>(1, c->max_column * permille / 1000);
     }
     nomad::AsyncLayout L;
-    RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, p.exact ? 1 : c->wpb, !p.exact, L,
-                                 threads));
+    const int32_t group = p.exact ? 1 : c->wpb;
+    if (dev_layout) {
+      // visit lists on the device from the device CSC; the host keeps the row blocks and
+      // builds the initial queues from each column's first visit
+      RC(nomad::async_layout_rows(train, c->P, p.balance, L, threads));
+      nomad::DeviceLayout t;
+      CK(nomad::device_layout_count(c->train, c->train_ptr, c->nnz_train, f.m, f.n, L.row_start.data(), c->P, group,
+                                    pri_min, &t, c->stream));
+      c->n_segments = t.nseg;
+      RC(dalloc(c, &c->segs, static_cast<size_t>(t.nseg)));
+      RC(dalloc(c, &c->vl_ptr, static_cast<size_t>(f.n) + 1));
+      L.vl_ptr.resize(static_cast<size_t>(f.n) + 1);
+      std::vector<nomad::Segment> firsts(static_cast<size_t>(f.n));
+      static_assert(sizeof(nomad::Segment) == sizeof(int4), "a visit is {start lo, start hi, len, owner}");
+      int32_t max_seg = 0;
+      CK(nomad::device_layout_fill(c->train, c->train_ptr, c->nnz_train, f.n, group, !p.exact, pri_min, p.seed, &t,
+                                   c->segs, c->vl_ptr, L.vl_ptr.data(), reinterpret_cast<int4*>(firsts.data()),
+                                   &max_seg, c->stream));
+      L.max_segment = max_seg;
+      nomad::async_layout_queues(train, pri_min, firsts.data(), L);
+      c->d2h_bytes += static_cast<int64_t>((static_cast<size_t>(f.n) + 1) * 8 + static_cast<size_t>(f.n) * 16);
+      if (p.debug_flags & 4) RC(check_device_layout(c, train, p, pri_min, group, L, threads));
+    } else {
+      RC(nomad::build_async_layout(train, c->P, p.balance, p.seed, pri_min, group, !p.exact, L, threads));
+      c->n_segments = static_cast<int64_t>(L.segs.size());
+    }
     trace.mark("async layout build");
     c->cta_heavy = cta_heavy && pri_min > 0;
     c->n_active = L.n_active;
     c->n_priority = L.n_priority;
-    c->n_segments = static_cast<int64_t>(L.segs.size());
     RC(upload(c, &c->tok_desc0, reinterpret_cast<const int4*>(L.desc0.data()), L.desc0.size() / 4));
     RC(dalloc(c, &c->tok_desc, std::max<size_t>(L.desc0.size() / 4, 1)));
     if (!p.exact) {
@@ -427,12 +482,14 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       RC(upload(c, &c->q_count, L.q_count.data(), L.q_count.size()));
     }
     RC(dalloc(c, &c->finish_ns, static_cast<size_t>(f.n) + 1));
-    RC(upload(c, &c->segs, reinterpret_cast<const int4*>(L.segs.data()), L.segs.size()));
-    if (!p.exact) {
-      RC(dalloc(c, &c->segx, 3 * std::max<size_t>(L.segs.size(), 1)));
-      CK(nomad::launch_build_segx(c->segs, c->train, static_cast<int64_t>(L.segs.size()), c->segx, c->stream));
+    if (!dev_layout) {
+      RC(upload(c, &c->segs, reinterpret_cast<const int4*>(L.segs.data()), L.segs.size()));
+      RC(upload(c, &c->vl_ptr, L.vl_ptr.data(), L.vl_ptr.size()));
     }
-    RC(upload(c, &c->vl_ptr, L.vl_ptr.data(), L.vl_ptr.size()));
+    if (!p.exact) {
+      RC(dalloc(c, &c->segx, 3 * std::max<size_t>(static_cast<size_t>(c->n_segments), 1)));
+      CK(nomad::launch_build_segx(c->segs, c->train, c->n_segments, c->segx, c->stream));
+    }
     RC(upload(c, &c->qnext0, L.qnext0.data(), L.qnext0.size()));
     RC(upload(c, &c->qtail0, L.qtail0.data(), L.qtail0.size()));
     RC(dalloc(c, &c->qnext, L.qnext0.size()));

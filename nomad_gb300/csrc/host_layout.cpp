@@ -180,13 +180,10 @@ int build_csc(const nomad_gpu_matrix& A, int32_t m, int32_t n, Csc& out, int thr
   return NOMAD_OK;
 }
 
-int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
-                       int64_t priority_min, int32_t group, bool group_routes, AsyncLayout& L,
-                       int threads) {
-  const int32_t m = csc.m, n = csc.n;
+int async_layout_rows(const Csc& csc, int32_t P, int balance, AsyncLayout& L, int threads) {
+  const int32_t m = csc.m;
   const int64_t nnz = csc.nnz();
   if (P <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker count must be positive");
-  if (group <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker group size must be positive");
   L.P = P;
   L.row_start.assign(static_cast<size_t>(P) + 1, m);
   if (balance == 0 || nnz == 0) {
@@ -222,6 +219,16 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     }
     for (; w <= P; ++w) L.row_start[w] = m;
   }
+  return NOMAD_OK;
+}
+
+int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
+                       int64_t priority_min, int32_t group, bool group_routes, AsyncLayout& L,
+                       int threads) {
+  const int32_t m = csc.m, n = csc.n;
+  if (group <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "worker group size must be positive");
+  int rc = async_layout_rows(csc, P, balance, L, threads);
+  if (rc) return rc;
   // visit lists: the rows of a column are ascending, so each worker's share is a run;
   // a priority column's visits are the runs of whole worker groups
   L.vl_ptr.assign(static_cast<size_t>(n) + 1, 0);
@@ -332,11 +339,24 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     }
   });
   L.max_segment = *std::max_element(maxseg.begin(), maxseg.end());
+  std::vector<Segment> firsts(static_cast<size_t>(n));
+  for (int32_t j = 0; j < n; ++j)
+    if (L.vl_ptr[j + 1] > L.vl_ptr[j]) firsts[j] = L.segs[L.vl_ptr[j]];
+  async_layout_queues(csc, priority_min, firsts.data(), L);
+  return NOMAD_OK;
+}
+
+void async_layout_queues(const Csc& csc, int64_t priority_min, const Segment* firsts, AsyncLayout& L) {
+  const int32_t n = csc.n, P = L.P;
+  auto is_priority = [&](int64_t j) {
+    return priority_min > 0 && csc.col_ptr[j + 1] - csc.col_ptr[j] >= priority_min;
+  };
+  auto nseg = [&](int32_t j) { return L.vl_ptr[j + 1] - L.vl_ptr[j]; };
   L.max_column = 0;
   L.n_active = 0;
   for (int32_t j = 0; j < n; ++j) {
     L.max_column = std::max<int64_t>(L.max_column, csc.col_ptr[j + 1] - csc.col_ptr[j]);
-    if (nseg[j] > 0) ++L.n_active;
+    if (nseg(j) > 0) ++L.n_active;
   }
   // initial queues: every active token at its first worker, in column order
   // (nb_main.cpp:82-97 pushes the tokens in index order); long columns go to the
@@ -350,8 +370,8 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
   L.q_count.assign(2 * static_cast<size_t>(P), 0);
   L.n_priority = 0;
   for (int32_t j = 0; j < n; ++j) {
-    if (nseg[j] == 0) continue;
-    const Segment& s0 = L.segs[L.vl_ptr[j]];
+    if (nseg(j) == 0) continue;
+    const Segment& s0 = firsts[j];
     const bool pri = is_priority(j);
     L.n_priority += pri ? 1 : 0;
     const int32_t q = (pri ? P : 0) + s0.worker;
@@ -367,13 +387,12 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
     fm[2] = s0.len;
     fm[3] = 0;
     fm[4] = 0;  // pass count, set per launch
-    fm[5] = static_cast<int32_t>(static_cast<uint32_t>(nseg[j]) | (pri ? 0x80000000u : 0u));
+    fm[5] = static_cast<int32_t>(static_cast<uint32_t>(nseg(j)) | (pri ? 0x80000000u : 0u));
     fm[6] = static_cast<int32_t>(static_cast<uint64_t>(L.vl_ptr[j]) & 0xffffffffu);
     fm[7] = static_cast<int32_t>(L.vl_ptr[j] >> 32);
     L.first_q[2 * static_cast<size_t>(j)] = q;
     L.first_q[2 * static_cast<size_t>(j) + 1] = L.q_count[q]++;
   }
-  return NOMAD_OK;
 }
 
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,

@@ -156,6 +156,35 @@ cudaError_t launch_drain_queues(const AsyncArgs& a, cudaStream_t s);
 cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_counts, const int32_t* cols,
                        const double* v64, const float* v32, int2* ratings, int64_t* col_ptr, int64_t* bad_col,
                        int32_t* dup_col, int64_t* h2d_bytes, cudaStream_t s);
+// The visit lists of the asynchronous modes built on the device (layout_device.cu) from a
+// device CSC, equal to the host's build_async_layout: count() takes the worker row blocks
+// (host row_start[P + 1]) and leaves the number of visits in t->nseg; fill() writes the
+// visits in route order (segs[nseg], {start lo, start hi, len, owner}) and the visit
+// offsets (vl_ptr[n + 1]) on the device, copies the offsets and each column's first
+// visit (firsts[n]) to the host, the longest visit to *max_seg, and frees t.  1 <= nnz <=
+// INT_MAX, 1 <= group <= 32.
+struct DeviceLayout {
+  int32_t* row_start = nullptr;
+  int32_t* row_worker = nullptr;
+  int32_t* flags = nullptr;
+  int32_t* seg_id = nullptr;
+  void* tmp = nullptr;
+  int64_t nseg = 0;
+};
+cudaError_t device_layout_count(const int2* ratings, const int64_t* col_ptr, int64_t nnz, int32_t m, int32_t n,
+                                const int32_t* row_start, int32_t P, int32_t group, int64_t priority_min,
+                                DeviceLayout* t, cudaStream_t s);
+cudaError_t device_layout_fill(const int2* ratings, const int64_t* col_ptr, int64_t nnz, int32_t n, int32_t group,
+                               bool group_routes, int64_t priority_min, uint64_t seed, DeviceLayout* t, int4* segs,
+                               int64_t* vl_ptr, int64_t* vl_ptr_host, int4* firsts_host, int32_t* max_seg,
+                               cudaStream_t s);
+void device_layout_release(DeviceLayout* t, cudaStream_t s);
+// Host-to-device copy of pageable memory through two pinned staging buffers kept for the
+// life of the process (32 MB each, allocated on first use; uploads are serialised by a
+// lock): host threads fill one while the copy engine drains the other.  Returns when the
+// copies are done.  Copies straight from pageable memory ran ~30x slower when the host
+// had been under heavy allocation beforehand.
+cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s);
 // The rows of a device CSC's ratings (nnz entries) copied to host memory.
 cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s);
 cudaError_t launch_build_segx(const int4* segs, const int2* ratings, int64_t nseg, int4* segx, cudaStream_t s);

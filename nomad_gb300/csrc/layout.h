@@ -130,6 +130,13 @@ int build_async_layout(const Csc& csc, int32_t P, int balance, uint64_t seed,
                        int64_t priority_min, int32_t group, bool group_routes, AsyncLayout& out,
                        int threads);
 
+// The two host parts of build_async_layout that a visit list built elsewhere
+// (layout_device.cu) still needs: the worker row blocks (L.P, L.row_start), and, from
+// each column's visit count (L.vl_ptr) and first visit in route order (firsts[n], read
+// only for active columns), the initial queues, first mailboxes and token counts.
+int async_layout_rows(const Csc& csc, int32_t P, int balance, AsyncLayout& L, int threads);
+void async_layout_queues(const Csc& csc, int64_t priority_min, const Segment* firsts, AsyncLayout& L);
+
 // innerB row blocks x col_blocks column blocks (innerB for DSGD, 2*innerB for
 // DSGD++: dsgdpp.cpp:42-52, 64-69); block (bi, bj) has id bi*col_blocks + bj.
 int build_dsgd_layout(const nomad_gpu_matrix& A, int32_t m, int32_t n, int32_t innerB,

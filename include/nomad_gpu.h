@@ -173,7 +173,13 @@ typedef struct nomad_gpu_ctx nomad_gpu_ctx; /* opaque */
 int nomad_gpu_params_default(nomad_gpu_params* p);
 
 /* Copy the problem to the device, build the layout and initialise W and H.  Host
- * buffers stay owned by the caller and are not referenced after the call. */
+ * buffers stay owned by the caller and are not referenced after the call.  Row-major
+ * rating sets (row_counts given, up to INT_MAX ratings) are sorted into column order on
+ * the device, and in ASYNC mode the visit lists are built there too; their arrays are
+ * copied in through two 32 MB pinned host buffers that the library allocates on first use
+ * and keeps for the life of the process.  Row counts are checked before any device work;
+ * column indices out of range and repeated (row, column) cells are refused
+ * (NOMAD_ERR_INVALID_ARG) before training starts. */
 int nomad_gpu_init(nomad_gpu_ctx** out, const nomad_gpu_problem* prob,
                    const nomad_gpu_params* params);
 

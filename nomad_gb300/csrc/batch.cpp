@@ -29,6 +29,8 @@ struct nomad_gpu_batch {
   nomad::BatchArgs a;
   int esz = 4;
   int grid = 0, sse_grid = 0;
+  std::vector<int32_t> part_of;   // per evaluation part: 2 * problem + set
+  std::vector<int64_t> set_count; // [2 * count] train and test ratings of each problem
   int32_t n_steps = 0, epochs_done = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -211,6 +213,22 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     }
   });
   csc_te.clear();
+  // the evaluation's parts: each problem's train and test ratings in runs of at most
+  // kSsePart, problems and sets in order
+  constexpr int64_t kSsePart = 32768;
+  std::vector<nomad::SsePart> parts;
+  b->set_count.assign(2 * static_cast<size_t>(count), 0);
+  for (int32_t i = 0; i < count; ++i)
+    for (int32_t set = 0; set < 2; ++set) {
+      const nomad::BatchProblem& pb = b->probs[i];
+      const std::vector<int64_t>& cpa = set ? tcp_all : cp_all;
+      const int64_t b0 = cpa[(set ? pb.test_col_off : pb.col_off)], e0 = cpa[(set ? pb.test_col_off : pb.col_off) + pb.n];
+      b->set_count[2 * static_cast<size_t>(i) + set] = e0 - b0;
+      for (int64_t s0 = b0; s0 < e0; s0 += kSsePart) {
+        parts.push_back(nomad::SsePart{s0, std::min(e0, s0 + kSsePart), i, set});
+        b->part_of.push_back(2 * i + set);
+      }
+    }
   trace.mark("concatenation");
   // work queue: the largest problems first, so the longest epochs start first
   std::vector<int32_t> order(count);
@@ -312,7 +330,11 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   RC(dalloc(b, &a.epoch, 1));
   RC(dalloc(b, &a.stats, 4));
   RC(dalloc(b, &a.err_sum, 1));
-  RC(dalloc(b, &a.sse, 4 * static_cast<size_t>(count)));
+  nomad::SsePart* dparts = nullptr;
+  RC(upload(b, &dparts, parts.data(), parts.size()));
+  a.parts = dparts;
+  a.n_parts = static_cast<int32_t>(parts.size());
+  RC(dalloc(b, &a.part_sse, std::max<size_t>(parts.size(), 1)));
   CK(cudaMemsetAsync(a.epoch, 0, sizeof(int32_t), b->stream));
   a.n_big = n_big;
   b->n_big = n_big;
@@ -389,7 +411,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   }
 
   trace.mark("factors");
-  b->sse_grid = std::max(1, std::min((count + 3) / 4, 8 * b->num_sms));
+  b->sse_grid = std::max(1, std::min((b->a.n_parts + 3) / 4, 8 * b->num_sms));
   RC(ensure_steps(b, 64));
   CK(cudaStreamSynchronize(b->stream));
   return NOMAD_OK;
@@ -470,13 +492,18 @@ int nomad_gpu_batch_rmse(nomad_gpu_batch* b, double* train_rmse, double* test_rm
   nomad::clear_last_error();
   if (!b) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "null batch");
   CK(cudaSetDevice(b->device));
-  CK(nomad::launch_batch_sse(b->a, b->sse_grid, b->stream));
-  std::vector<double> s(4 * static_cast<size_t>(b->a.count));
-  CK(cudaMemcpyAsync(s.data(), b->a.sse, s.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
-  CK(cudaStreamSynchronize(b->stream));
+  const size_t np = b->part_of.size();
+  std::vector<double> part(np), sse(2 * static_cast<size_t>(b->a.count), 0.0);
+  if (np) {
+    CK(nomad::launch_batch_sse(b->a, b->sse_grid, b->stream));
+    CK(cudaMemcpyAsync(part.data(), b->a.part_sse, np * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+  }
+  for (size_t k = 0; k < np; ++k) sse[b->part_of[k]] += part[k];  // a problem's parts in order
   for (int32_t i = 0; i < b->a.count; ++i) {
-    if (train_rmse) train_rmse[i] = s[4 * i + 1] > 0 ? std::sqrt(s[4 * i] / s[4 * i + 1]) : 0.0;
-    if (test_rmse) test_rmse[i] = s[4 * i + 3] > 0 ? std::sqrt(s[4 * i + 2] / s[4 * i + 3]) : 0.0;
+    const int64_t ntr = b->set_count[2 * static_cast<size_t>(i)], nte = b->set_count[2 * static_cast<size_t>(i) + 1];
+    if (train_rmse) train_rmse[i] = ntr > 0 ? std::sqrt(sse[2 * i] / static_cast<double>(ntr)) : 0.0;
+    if (test_rmse) test_rmse[i] = nte > 0 ? std::sqrt(sse[2 * i + 1] / static_cast<double>(nte)) : 0.0;
   }
   return NOMAD_OK;
 }

@@ -517,39 +517,48 @@ __global__ void batch_advance_kernel(int32_t* epoch, int32_t* next) {
   *next = 0;
 }
 
-// Per-problem FP64 squared errors of the train and the test ratings, a warp per problem.
+// FP64 squared errors of the evaluation's parts, a warp per part: the part's first column
+// by a binary search of its problem's column offsets, then rating by rating, the column
+// reloaded as it changes.  (A warp per whole problem left the largest problems' millions
+// of ratings on one warp each.)  The host adds the parts of a problem in order.
 template <typename Store>
 __global__ void __launch_bounds__(nomad::kBatchThreads) batch_sse_kernel(nomad::BatchArgs a) {
   constexpr int NV = 1;
   constexpr int E = Vec<Store>::E;
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int prob = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); prob < a.count; prob += warps) {
-    const nomad::BatchProblem pb = a.problems[prob];
+  for (int part = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); part < a.n_parts; part += warps) {
+    const nomad::SsePart pt = a.parts[part];
+    const nomad::BatchProblem pb = a.problems[pt.prob];
     const nomad::DevFactors f = batch_factors(a, pb, static_cast<int>(sizeof(Store)));
     const Store* __restrict__ W = static_cast<const Store*>(f.W);
     const Store* __restrict__ H = static_cast<const Store*>(f.H);
-    for (int set = 0; set < 2; ++set) {
-      const int2* rt = set ? a.test : a.ratings;
-      const int64_t* cp = set ? a.test_col_ptr + pb.test_col_off : a.col_ptr + pb.col_off;
-      double acc = 0.0;
-      for (int j = 0; j < pb.n; ++j) {
-        float h[NV][E];
-        load_col<Store, NV>(H, j, f, lane, h);
-        for (int64_t o = cp[j]; o < cp[j + 1]; ++o) {
-          const int2 r = __ldg(&rt[o]);
-          float w[NV][E];
-          load_row<Store, NV>(W, r.x, f.kpad, f.nvec, lane, w);
-          const float err = rating_error<Store, NV, false>(h, w, __int_as_float(r.y), f.nvec, f.red_width, f.dim,
-                                                           lane, nullptr);
-          acc += static_cast<double>(err) * err;
-        }
-      }
-      if (lane == 0) {
-        a.sse[4 * static_cast<int64_t>(prob) + 2 * set] = acc;
-        a.sse[4 * static_cast<int64_t>(prob) + 2 * set + 1] = static_cast<double>(cp[pb.n] - cp[0]);
-      }
+    const int2* rt = pt.set ? a.test : a.ratings;
+    const int64_t* cp = pt.set ? a.test_col_ptr + pb.test_col_off : a.col_ptr + pb.col_off;
+    int lo = 0, hi = pb.n;  // the last column j with cp[j] <= start (cp[0] <= start < cp[n])
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (cp[mid] <= pt.start) lo = mid;
+      else hi = mid;
     }
+    int j = lo;
+    float h[NV][E];
+    load_col<Store, NV>(H, j, f, lane, h);
+    double acc = 0.0;
+    for (int64_t o = pt.start; o < pt.end; ++o) {
+      if (cp[j + 1] <= o) {
+        do ++j;
+        while (cp[j + 1] <= o);
+        load_col<Store, NV>(H, j, f, lane, h);
+      }
+      const int2 r = __ldg(&rt[o]);
+      float w[NV][E];
+      load_row<Store, NV>(W, r.x, f.kpad, f.nvec, lane, w);
+      const float err = rating_error<Store, NV, false>(h, w, __int_as_float(r.y), f.nvec, f.red_width, f.dim,
+                                                       lane, nullptr);
+      acc += static_cast<double>(err) * err;
+    }
+    if (lane == 0) a.part_sse[part] = acc;
   }
 }
 

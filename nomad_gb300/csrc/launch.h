@@ -97,6 +97,13 @@ static_assert(sizeof(BatchProblem) == 80, "batch problem entry");
 constexpr int kBatchWorkers = 16;
 constexpr int kBatchRing = 8192;  // ring capacity: a large problem has at most 5,000 + columns
 
+// A part of one problem's train (set 0) or test (set 1) ratings for the evaluation:
+// absolute offsets [start, end) into that set's concatenated ratings.
+struct SsePart {
+  int64_t start, end;
+  int32_t prob, set;
+};
+
 struct BatchArgs {
   void* W = nullptr;  // every problem's rows, concatenated
   void* H = nullptr;
@@ -116,7 +123,9 @@ struct BatchArgs {
   int32_t bf16 = 0, exact = 0;
   unsigned long long* stats = nullptr;  // [0] updates
   double* err_sum = nullptr;            // [1] online squared error
-  double* sse = nullptr;                // [4 * count] train SSE, train count, test SSE, test count
+  const SsePart* parts = nullptr;       // the evaluation's parts, problems and sets in order
+  int32_t n_parts = 0;
+  double* part_sse = nullptr;           // [n_parts] FP64 squared-error sum of each part
   // large problems: the first n_big entries of `order`, taken a block at a time
   int32_t n_big = 0;
   int32_t* next_big = nullptr;          // [1] large-problem queue head

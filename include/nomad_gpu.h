@@ -100,7 +100,8 @@ typedef struct nomad_gpu_params {
                         * visit (the others' join wait runs out: a timeout);          *
                         * bit 2 = ASYNC: build the visit lists on the host as well as *
                         * on the device and refuse with NOMAD_ERR_BOUNDS if they      *
-                        * differ                                                      */
+                        * differ; batched form: the same for the CSCs and the large   *
+                        * problems' visit bounds                                      */
   int32_t long_visit;  /* ASYNC: visits with at least this many ratings run the blocked
                           (7-rating) path with TMA-staged rows; 0 = default 14        */
   int32_t priority_permille; /* ASYNC: columns with at least this many permille of the
@@ -323,7 +324,9 @@ int nomad_gpu_sse_noalloc(int32_t device, int32_t precision, int32_t n, int32_t 
  * one-worker replay bit for bit; otherwise FMA arithmetic, FP32 or BF16_SR storage.
  * Uses params.precision, exact, lrate, drate, reg, seed, init_parts, device; dim comes
  * per problem (at most 128).  No counterpart in the reference (it trains one problem
- * per run). */
+ * per run).  When every set is row-major with one value type, the CSCs of all
+ * problems are built on the device in one sort (else on the host, problem by problem);
+ * a column out of range or a repeated cell is refused either way, naming the problem. */
 typedef struct nomad_gpu_batch_problem {
   int32_t m, n, dim, reserved;
   nomad_gpu_matrix train, test; /* as in nomad_gpu_problem                             */

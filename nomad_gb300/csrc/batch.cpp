@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -121,6 +123,40 @@ int ensure_graph(nomad_gpu_batch* b) {
   return NOMAD_OK;
 }
 
+// Whether the device build takes every problem's sets: each row-major or empty, one value
+// type throughout (*f64), the totals within its limits.
+bool device_batch_ok(const nomad_gpu_batch_problem* P, int32_t count, bool* f64) {
+  int kind = 0;  // 1: fp64 values, 2: fp32
+  int64_t tr = 0, te = 0, rows = 0, cols = 0;
+  for (int32_t i = 0; i < count; ++i) {
+    for (const nomad_gpu_matrix* A : {&P[i].train, &P[i].test}) {
+      if (A->nnz == 0) continue;
+      if (A->nnz < 0 || !A->row_counts || !A->cols || (A->vals_f64 != nullptr) == (A->vals_f32 != nullptr))
+        return false;
+      const int k = A->vals_f64 ? 1 : 2;
+      if (kind && k != kind) return false;
+      kind = k;
+    }
+    tr += std::max<int64_t>(P[i].train.nnz, 0);
+    te += std::max<int64_t>(P[i].test.nnz, 0);
+    rows += P[i].m;
+    cols += P[i].n;
+  }
+  *f64 = kind == 1;
+  return kind != 0 && tr <= INT_MAX && te <= INT_MAX && rows < INT_MAX && cols <= INT_MAX;
+}
+
+// Compares `bytes` of device memory with a host copy; the first difference names *differs.
+int same_as_device(nomad_gpu_batch* b, const void* dev, const void* host, size_t bytes, const char* what,
+                   const char** differs) {
+  if (*differs || bytes == 0) return NOMAD_OK;
+  std::vector<char> got(bytes);
+  CK(cudaMemcpyAsync(got.data(), dev, bytes, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (std::memcmp(got.data(), host, bytes) != 0) *differs = what;
+  return NOMAD_OK;
+}
+
 int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t count) {
   const nomad_gpu_params& p = b->prm;
   const int threads = nomad::host_threads();
@@ -139,34 +175,18 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   b->esz = bf16 ? 2 : 4;
 
   // ---- per-problem layout, concatenated ------------------------------------------------
-  // Each problem's CSC is built on one thread, problems handed out on demand; the
-  // concatenated arrays are then sized by prefix sums and filled in parallel.
+  // The sets are built into CSC on the device in one sort of every problem's entries
+  // (csc_device.cu) when every set is row-major; else, and to name a fault the device
+  // build found, each problem's CSC is built on one host thread and the results are
+  // concatenated.
   b->probs.resize(count);
   for (int32_t i = 0; i < count; ++i) {
     const nomad_gpu_batch_problem& q = P[i];
     if (q.m <= 0 || q.n <= 0) NOMAD_FAIL(NOMAD_ERR_INVALID_ARG, "problem %d: m and n must be positive", i);
     if (q.dim <= 0 || q.dim > 128) NOMAD_FAIL(NOMAD_ERR_UNSUPPORTED, "problem %d: dim %d outside [1, 128]", i, q.dim);
   }
-  std::vector<nomad::Csc> csc_tr(count), csc_te(count);
-  std::vector<int> status(count, NOMAD_OK);
-  std::vector<std::string> errors(count);
-  nomad::parallel_dynamic(count, 4, threads, [&](int, int64_t lo, int64_t hi) {
-    for (int64_t i = lo; i < hi; ++i) {
-      const nomad_gpu_batch_problem& q = P[i];
-      int rc = nomad::build_csc(q.train, q.m, q.n, csc_tr[i], 1);
-      if (!rc) rc = nomad::build_csc(q.test, q.m, q.n, csc_te[i], 1);
-      if (rc) {
-        status[i] = rc;
-        errors[i] = nomad::last_error();
-      }
-    }
-  });
-  for (int32_t i = 0; i < count; ++i)
-    if (status[i]) NOMAD_FAIL(status[i], "problem %d: %s", i, errors[i].c_str());
-  trace.mark("CSC builds");
-  std::vector<int64_t> nnz(count);
+  std::vector<int64_t> nnz(count), nnz_te(count);
   int64_t w_off = 0, h_off = 0, tr_len = 0, te_len = 0, cp_len = 0, tcp_len = 0;
-  int64_t max_rows = 0;
   std::vector<int64_t> tr_at(count), te_at(count);
   for (int32_t i = 0; i < count; ++i) {
     const nomad_gpu_batch_problem& q = P[i];
@@ -183,36 +203,111 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
     pb.h_off = h_off;
     w_off += static_cast<int64_t>(q.m) * pb.kpad;
     h_off += static_cast<int64_t>(q.n) * pb.kpad;
-    max_rows = std::max<int64_t>(max_rows, std::max(q.m, q.n));
     pb.col_off = cp_len;
     pb.test_col_off = tcp_len;
     cp_len += q.n + 1;
     tcp_len += q.n + 1;
     tr_at[i] = tr_len;
     te_at[i] = te_len;
-    nnz[i] = csc_tr[i].nnz();
+    nnz[i] = std::max<int64_t>(q.train.nnz, 0);  // a negative count fails the checks below
+    nnz_te[i] = std::max<int64_t>(q.test.nnz, 0);
     tr_len += nnz[i];
-    te_len += csc_te[i].nnz();
+    te_len += nnz_te[i];
   }
-  std::vector<nomad::Rating, nomad::NoInitAllocator<nomad::Rating>> tr_all(tr_len), te_all(te_len);  // device int2
-  std::vector<int64_t> cp_all(cp_len), tcp_all(tcp_len);
-  nomad::parallel_dynamic(count, 4, threads, [&](int, int64_t lo, int64_t hi) {
-    for (int64_t i = lo; i < hi; ++i) {
-      nomad::BatchProblem& pb = b->probs[i];
-      const nomad::Csc& tr = csc_tr[i];
-      const nomad::Csc& te = csc_te[i];
-      for (int32_t j = 0; j <= pb.n; ++j) {
-        cp_all[pb.col_off + j] = tr_at[i] + tr.col_ptr[j];
-        tcp_all[pb.test_col_off + j] = te_at[i] + te.col_ptr[j];
+  bool f64 = false;
+  bool on_device = device_batch_ok(P, count, &f64);
+  if (on_device) {  // the checks of the host build that need no sort
+    std::atomic<bool> ok{true};
+    nomad::parallel_dynamic(count, 16, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi && ok.load(std::memory_order_relaxed); ++i)
+        if (nomad::check_rating_set(P[i].train, P[i].m, P[i].n, 1, false) ||
+            nomad::check_rating_set(P[i].test, P[i].m, P[i].n, 1, false))
+          ok = false;
+    });
+    on_device = ok;
+  }
+  int2 *tr = nullptr, *te = nullptr;
+  int64_t *cp = nullptr, *tcp = nullptr;
+  RC(dalloc(b, &tr, static_cast<size_t>(tr_len)));
+  RC(dalloc(b, &te, static_cast<size_t>(te_len)));
+  RC(dalloc(b, &cp, static_cast<size_t>(cp_len)));
+  RC(dalloc(b, &tcp, static_cast<size_t>(tcp_len)));
+  std::vector<int32_t> active(count, 0);
+  bool built = false;
+  if (on_device) {
+    std::vector<nomad::BatchSetIn> in(count);
+    auto sets = [&](int test) {
+      for (int32_t i = 0; i < count; ++i) {
+        const nomad_gpu_matrix& A = test ? P[i].test : P[i].train;
+        in[i] = nomad::BatchSetIn{A.nnz, P[i].m, P[i].n, A.row_counts, A.cols,
+                                  f64 ? static_cast<const void*>(A.vals_f64) : static_cast<const void*>(A.vals_f32)};
       }
-      std::copy(tr.ratings.begin(), tr.ratings.end(), tr_all.begin() + tr_at[i]);
-      std::copy(te.ratings.begin(), te.ratings.end(), te_all.begin() + te_at[i]);
-      int32_t act = 0;
-      for (int32_t j = 0; j < pb.n; ++j) act += tr.col_ptr[j + 1] > tr.col_ptr[j] ? 1 : 0;
-      pb.n_active = act;
+      return in.data();
+    };
+    bool faulty = false;
+    int64_t h2d = 0;
+    CK(nomad::device_batch_csc(sets(0), count, f64, tr, cp, active.data(), &faulty, &h2d, b->stream));
+    if (!faulty) CK(nomad::device_batch_csc(sets(1), count, f64, te, tcp, nullptr, &faulty, &h2d, b->stream));
+    built = !faulty;
+    trace.mark("CSC builds (device)");
+  }
+  std::vector<nomad::Csc> csc_tr;  // the host builds, when made
+  if (!built || (p.debug_flags & 4)) {
+    std::vector<nomad::Csc> csc_te(count);
+    csc_tr.resize(count);
+    std::vector<int> status(count, NOMAD_OK);
+    std::vector<std::string> errors(count);
+    nomad::parallel_dynamic(count, 4, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi; ++i) {
+        const nomad_gpu_batch_problem& q = P[i];
+        int rc = nomad::build_csc(q.train, q.m, q.n, csc_tr[i], 1);
+        if (!rc) rc = nomad::build_csc(q.test, q.m, q.n, csc_te[i], 1);
+        if (rc) {
+          status[i] = rc;
+          errors[i] = nomad::last_error();
+        }
+      }
+    });
+    for (int32_t i = 0; i < count; ++i)
+      if (status[i]) NOMAD_FAIL(status[i], "problem %d: %s", i, errors[i].c_str());
+    if (built) trace.mark("CSC builds (host, for the check)");
+    else trace.mark("CSC builds (host)");
+    std::vector<nomad::Rating, nomad::NoInitAllocator<nomad::Rating>> tr_all(tr_len), te_all(te_len);
+    std::vector<int64_t> cp_all(cp_len), tcp_all(tcp_len);
+    std::vector<int32_t> act(count, 0);
+    nomad::parallel_dynamic(count, 4, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi; ++i) {
+        const nomad::BatchProblem& pb = b->probs[i];
+        const nomad::Csc& c = csc_tr[i];
+        const nomad::Csc& t = csc_te[i];
+        for (int32_t j = 0; j <= pb.n; ++j) {
+          cp_all[pb.col_off + j] = tr_at[i] + c.col_ptr[j];
+          tcp_all[pb.test_col_off + j] = te_at[i] + t.col_ptr[j];
+        }
+        std::copy(c.ratings.begin(), c.ratings.end(), tr_all.begin() + tr_at[i]);
+        std::copy(t.ratings.begin(), t.ratings.end(), te_all.begin() + te_at[i]);
+        for (int32_t j = 0; j < pb.n; ++j) act[i] += c.col_ptr[j + 1] > c.col_ptr[j] ? 1 : 0;
+      }
+    });
+    static_assert(sizeof(nomad::Rating) == sizeof(int2), "rating layout");
+    if (!built) {
+      CK(nomad::upload_staged(tr, tr_all.data(), tr_all.size() * sizeof(int2), b->stream));
+      CK(nomad::upload_staged(te, te_all.data(), te_all.size() * sizeof(int2), b->stream));
+      CK(nomad::upload_staged(cp, cp_all.data(), cp_all.size() * sizeof(int64_t), b->stream));
+      CK(nomad::upload_staged(tcp, tcp_all.data(), tcp_all.size() * sizeof(int64_t), b->stream));
+      active = act;
+    } else {  // debug bit 2: the device build must equal the host's, entry for entry
+      const char* differs = nullptr;
+      RC(same_as_device(b, tr, tr_all.data(), tr_all.size() * sizeof(int2), "train ratings", &differs));
+      RC(same_as_device(b, te, te_all.data(), te_all.size() * sizeof(int2), "test ratings", &differs));
+      RC(same_as_device(b, cp, cp_all.data(), cp_all.size() * sizeof(int64_t), "train column pointers", &differs));
+      RC(same_as_device(b, tcp, tcp_all.data(), tcp_all.size() * sizeof(int64_t), "test column pointers", &differs));
+      if (!differs && act != active) differs = "columns with ratings";
+      if (differs) NOMAD_FAIL(NOMAD_ERR_BOUNDS, "device batch CSC differs from the host build: %s", differs);
     }
-  });
-  csc_te.clear();
+    trace.mark("concatenation", b->stream);
+  }
+  for (int32_t i = 0; i < count; ++i) b->probs[i].n_active = active[i];
   // the evaluation's parts: each problem's train and test ratings in runs of at most
   // kSsePart, problems and sets in order
   constexpr int64_t kSsePart = 32768;
@@ -220,16 +315,13 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   b->set_count.assign(2 * static_cast<size_t>(count), 0);
   for (int32_t i = 0; i < count; ++i)
     for (int32_t set = 0; set < 2; ++set) {
-      const nomad::BatchProblem& pb = b->probs[i];
-      const std::vector<int64_t>& cpa = set ? tcp_all : cp_all;
-      const int64_t b0 = cpa[(set ? pb.test_col_off : pb.col_off)], e0 = cpa[(set ? pb.test_col_off : pb.col_off) + pb.n];
+      const int64_t b0 = set ? te_at[i] : tr_at[i], e0 = b0 + (set ? nnz_te[i] : nnz[i]);
       b->set_count[2 * static_cast<size_t>(i) + set] = e0 - b0;
       for (int64_t s0 = b0; s0 < e0; s0 += kSsePart) {
         parts.push_back(nomad::SsePart{s0, std::min(e0, s0 + kSsePart), i, set});
         b->part_of.push_back(2 * i + set);
       }
     }
-  trace.mark("concatenation");
   // work queue: the largest problems first, so the longest epochs start first
   std::vector<int32_t> order(count);
   std::iota(order.begin(), order.end(), 0);
@@ -251,30 +343,33 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
                                     : std::max<int64_t>(8192, share * total / std::max<int64_t>(warps, 1));
   int32_t n_big = 0;
   constexpr int R = nomad::kBatchWorkers;
-  std::vector<int32_t> rs_all;
-  std::vector<int64_t> seg_all;
+  int32_t* rs_d = nullptr;
+  int64_t* seg_d = nullptr;
   if (!p.exact) {
     while (n_big < count && nnz[order[n_big]] >= big_min && P[order[n_big]].n < nomad::kBatchRing &&
            P[order[n_big]].n < 65536)
       ++n_big;
-    // slices: R + 1 row starts and n (R + 1) visit offsets per large problem
+  }
+  if (n_big > 0) {
+    // slices: R + 1 row starts per large problem from its row counts (equal rating counts
+    // per warp), and n (R + 1) visit bounds, found on the device
+    std::vector<nomad::BatchSegIn> big(n_big);
     int64_t seg_len = 0;
     for (int32_t t = 0; t < n_big; ++t) {
       nomad::BatchProblem& pb = b->probs[order[t]];
       pb.rs_off = t * (R + 1);
       pb.seg_off = seg_len;
+      big[t] = nomad::BatchSegIn{pb.col_off, pb.seg_off, pb.n, pb.rs_off};
       seg_len += static_cast<int64_t>(pb.n) * (R + 1);
     }
-    rs_all.assign(static_cast<size_t>(n_big) * (R + 1), 0);
-    seg_all.assign(static_cast<size_t>(seg_len), 0);
+    std::vector<int32_t> rs_all(static_cast<size_t>(n_big) * (R + 1), 0);
     nomad::parallel_dynamic(n_big, 1, threads, [&](int, int64_t lo, int64_t hi) {
       for (int64_t t = lo; t < hi; ++t) {
         const int32_t i = order[t];
-        const nomad::Csc& c = csc_tr[i];
         const nomad::BatchProblem& pb = b->probs[i];
-        const std::vector<int32_t>& row_nnz = c.row_nnz;  // ratings per row, from the CSC build
+        const int32_t* row_nnz = built ? P[i].train.row_counts : csc_tr[i].row_nnz.data();
         int32_t* rs = rs_all.data() + pb.rs_off;
-        const int64_t nz = c.nnz();
+        const int64_t nz = nnz[i];
         int64_t acc = 0;
         int32_t r = 1;
         rs[0] = 0;
@@ -283,20 +378,35 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
           while (r < R && acc >= (nz * r + R - 1) / R) rs[r++] = row + 1;
         }
         for (; r <= R; ++r) rs[r] = pb.m;
-        const int64_t cbase = cp_all[pb.col_off];  // absolute offset of the problem's ratings
-        int64_t* sg = seg_all.data() + pb.seg_off;
-        for (int32_t j = 0; j < pb.n; ++j) {
-          int64_t o = c.col_ptr[j];
-          for (int32_t w = 0; w <= R; ++w) {
-            while (o < c.col_ptr[j + 1] && c.ratings[o].row < rs[w]) ++o;
-            *sg++ = cbase + o;
-          }
-        }
       }
     });
+    RC(upload(b, &rs_d, rs_all.data(), rs_all.size()));
+    RC(dalloc(b, &seg_d, static_cast<size_t>(seg_len)));
+    CK(nomad::device_batch_segs(tr, cp, big.data(), n_big, rs_d, R, seg_d, b->stream));
+    if (!csc_tr.empty() && built) {  // debug bit 2: the bounds as the host finds them
+      std::vector<int64_t> seg_all(static_cast<size_t>(seg_len));
+      nomad::parallel_dynamic(n_big, 1, threads, [&](int, int64_t lo, int64_t hi) {
+        for (int64_t t = lo; t < hi; ++t) {
+          const nomad::BatchProblem& pb = b->probs[order[t]];
+          const nomad::Csc& c = csc_tr[order[t]];
+          const int32_t* rs = rs_all.data() + pb.rs_off;
+          int64_t* sg = seg_all.data() + pb.seg_off;
+          for (int32_t j = 0; j < pb.n; ++j) {
+            int64_t o = c.col_ptr[j];
+            for (int32_t w = 0; w <= R; ++w) {
+              while (o < c.col_ptr[j + 1] && c.ratings[o].row < rs[w]) ++o;
+              *sg++ = tr_at[order[t]] + o;
+            }
+          }
+        }
+      });
+      const char* differs = nullptr;
+      RC(same_as_device(b, seg_d, seg_all.data(), seg_all.size() * sizeof(int64_t), "visit bounds", &differs));
+      if (differs) NOMAD_FAIL(NOMAD_ERR_BOUNDS, "device batch CSC differs from the host build: %s", differs);
+    }
   }
   csc_tr.clear();
-  trace.mark("large-problem layout");
+  trace.mark("large-problem layout", b->stream);
 
   nomad::BatchArgs& a = b->a;
   a.count = count;
@@ -309,15 +419,8 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   RC(dalloc(b, &H, static_cast<size_t>(h_off) * b->esz));
   a.W = W;
   a.H = H;
-  int2 *tr = nullptr, *te = nullptr;
-  int64_t *cp = nullptr, *tcp = nullptr;
   nomad::BatchProblem* dp = nullptr;
   int32_t* dord = nullptr;
-  static_assert(sizeof(nomad::Rating) == sizeof(int2), "rating layout");
-  RC(upload(b, &tr, reinterpret_cast<const int2*>(tr_all.data()), tr_all.size()));
-  RC(upload(b, &te, reinterpret_cast<const int2*>(te_all.data()), te_all.size()));
-  RC(upload(b, &cp, cp_all.data(), cp_all.size()));
-  RC(upload(b, &tcp, tcp_all.data(), tcp_all.size()));
   RC(upload(b, &dp, b->probs.data(), b->probs.size()));
   RC(upload(b, &dord, order.data(), order.size()));
   a.ratings = tr;
@@ -345,12 +448,8 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   CK(cudaMemcpyAsync(a.next, &a.n_big, sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));  // small ones after
   a.budget_ns = static_cast<int64_t>(std::max(p.spin_budget_ms, 1)) * 1000000LL;
   if (n_big > 0) {
-    int32_t* rs = nullptr;
-    int64_t* sg = nullptr;
-    RC(upload(b, &rs, rs_all.data(), rs_all.size()));
-    RC(upload(b, &sg, seg_all.data(), seg_all.size()));
-    a.row_start = rs;
-    a.seg = sg;
+    a.row_start = rs_d;
+    a.seg = seg_d;
     RC(dalloc(b, &a.rings, static_cast<size_t>(b->grid) * R * nomad::kBatchRing));
     RC(dalloc(b, &a.ring_ctr, static_cast<size_t>(b->grid) * R));
     CK(cudaMemsetAsync(a.rings, 0xff, static_cast<size_t>(b->grid) * R * nomad::kBatchRing * 8, b->stream));

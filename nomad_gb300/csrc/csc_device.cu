@@ -2,7 +2,8 @@
 // set-up: the entries are copied in as they are (row counts, column indices, values),
 // sorted by column with a stable radix sort -- rows stay ascending inside a column, as
 // the host build (host_layout.cpp: build_csc) and the reference's read_data leave them
-// (Code/nomad/nb_data.cpp:131-169) -- and left in place for the kernels.
+// (Code/nomad/nb_data.cpp:131-169) -- and left in place for the kernels.  A batch of
+// problems is sorted in one pass, keyed by (problem, column).
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -18,7 +19,7 @@
 namespace {
 
 // Row counts as int64, with a zero after the last row (its exclusive sum is row_ptr).
-__global__ void counts64_kernel(const int32_t* rc, int32_t m, int64_t* out) {
+__global__ void counts64_kernel(const int32_t* rc, int64_t m, int64_t* out) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i <= m) out[i] = i < m ? rc[i] : 0;
 }
@@ -62,6 +63,83 @@ __global__ void rows_kernel(const int2* ratings, int64_t nnz, int32_t* rows) {
   if (i < nnz) rows[i] = ratings[i].x;
 }
 
+// The last p with at[p] <= x, for at[0] = 0 <= x < at[count] and at increasing.
+__device__ __forceinline__ int32_t owner_of(const int64_t* at, int32_t count, int64_t x) {
+  int32_t lo = 0, hi = count;
+  while (hi - lo > 1) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (at[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Batched sets, one warp per row of the concatenated row-major entries: row r of problem
+// p gives each of its entries the key colbase[p] + column and the pair {local row, value
+// as fp32}; the first entry with a column outside [0, n_p) goes to *bad.
+__global__ void batch_expand_kernel(const int64_t* row_ptr, int64_t rows, const int64_t* row_at,
+                                    const int64_t* colbase, int32_t count, const uint32_t* cols, const double* v64,
+                                    const float* v32, uint32_t* keys, int2* pairs, unsigned long long* bad) {
+  const int64_t r = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= rows) return;
+  const int32_t p = owner_of(row_at, count, r);
+  const int64_t base = colbase[p];
+  const uint32_t n = static_cast<uint32_t>(colbase[p + 1] - base);
+  const int32_t local = static_cast<int32_t>(r - row_at[p]);
+  const int64_t b = row_ptr[r], e = row_ptr[r + 1];
+  for (int64_t i = b + lane; i < e; i += 32) {
+    const uint32_t c = cols[i];
+    if (c >= n) atomicMin(bad, static_cast<unsigned long long>(i));
+    keys[i] = c < n ? static_cast<uint32_t>(base + c) : 0u;
+    const float v = v64 ? static_cast<float>(v64[i]) : v32[i];
+    pairs[i] = make_int2(local, __float_as_int(v));
+  }
+}
+
+// Each problem's n + 1 column pointers out of the global ones (col_ptr over all problems'
+// columns): entry t of the output is column t - cpo[p] of the problem p it falls in.
+__global__ void batch_col_ptr_kernel(const int64_t* gptr, const int64_t* cpo, const int64_t* colbase, int32_t count,
+                                     int64_t total, int64_t* col_ptr) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int32_t p = owner_of(cpo, count, t);
+  col_ptr[t] = gptr[colbase[p] + (t - cpo[p])];
+}
+
+// One block per problem: its columns with at least one rating.
+__global__ void batch_active_kernel(const int64_t* gptr, const int64_t* colbase, int32_t* act) {
+  const int64_t b = colbase[blockIdx.x], e = colbase[blockIdx.x + 1];
+  int c = 0;
+  for (int64_t j0 = b; j0 < e; j0 += blockDim.x) {
+    const int64_t j = j0 + threadIdx.x;
+    c += __syncthreads_count(j < e && gptr[j + 1] > gptr[j]);
+  }
+  if (threadIdx.x == 0) act[blockIdx.x] = c;
+}
+
+// One block per large problem, a thread per column: the R + 1 visit bounds of the column
+// (rows ascend inside it, so each bound is a lower bound from the previous one).
+__global__ void batch_segs_kernel(const int2* ratings, const int64_t* col_ptr, const nomad::BatchSegIn* big,
+                                  const int32_t* rs, int32_t R, int64_t* seg) {
+  const nomad::BatchSegIn g = big[blockIdx.x];
+  for (int32_t j = threadIdx.x; j < g.n; j += blockDim.x) {
+    int64_t o = col_ptr[g.col_off + j];
+    const int64_t e = col_ptr[g.col_off + j + 1];
+    int64_t* out = seg + g.seg_off + static_cast<int64_t>(j) * (R + 1);
+    for (int32_t w = 0; w <= R; ++w) {
+      const int32_t bound = rs[g.rs_off + w];
+      int64_t hi = e;
+      while (o < hi) {
+        const int64_t mid = o + ((hi - o) >> 1);
+        if (ratings[mid].x < bound) o = mid + 1;
+        else hi = mid;
+      }
+      out[w] = o;
+    }
+  }
+}
+
 // Two pinned staging buffers for uploads from pageable memory, kept for the life of the
 // process and used under a lock.
 constexpr size_t kStageBytes = size_t{32} << 20;
@@ -73,7 +151,29 @@ char* g_stage[2] = {nullptr, nullptr};
 namespace nomad {
 
 cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
-  if (bytes == 0) return cudaSuccess;
+  return upload_staged_many(dst, &src, &bytes, 1, s);
+}
+
+cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t* bytes, size_t count,
+                               cudaStream_t s) {
+  // pieces of at most 1 MB, none across a staging window
+  struct Piece {
+    const char* src;
+    size_t at, len;
+  };
+  std::vector<Piece> pieces;
+  size_t total = 0;
+  for (size_t i = 0; i < count; ++i) {
+    const char* p = static_cast<const char*>(srcs[i]);
+    for (size_t left = bytes[i]; left > 0;) {
+      const size_t len = std::min({left, kStageBytes - total % kStageBytes, size_t{1} << 20});
+      pieces.push_back(Piece{p, total, len});
+      p += len;
+      total += len;
+      left -= len;
+    }
+  }
+  if (total == 0) return cudaSuccess;
   std::lock_guard<std::mutex> lock(g_stage_mu);
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 2 && e == cudaSuccess; ++i)
@@ -82,18 +182,22 @@ cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
   const int threads = host_threads();
   bool used[2] = {false, false};
-  for (size_t off = 0, k = 0; off < bytes && e == cudaSuccess; off += kStageBytes, k ^= 1) {
-    const size_t n = std::min(kStageBytes, bytes - off);
+  size_t first = 0;  // the window's first piece
+  for (size_t off = 0, k = 0; off < total && e == cudaSuccess; off += kStageBytes, k ^= 1) {
+    const size_t n = std::min(kStageBytes, total - off);
+    size_t last = first;
+    while (last < pieces.size() && pieces[last].at < off + n) ++last;
     if (used[k]) e = cudaEventSynchronize(done[k]);  // the copy out of this buffer is done
     if (e != cudaSuccess) break;
-    const char* from = static_cast<const char*>(src) + off;
     char* to = g_stage[k];
-    const int64_t pieces = static_cast<int64_t>((n + (size_t{1} << 20) - 1) >> 20);
-    parallel_chunks(pieces, threads, [&](int, int64_t lo, int64_t hi) {
-      const size_t a = static_cast<size_t>(lo) << 20, b = std::min(n, static_cast<size_t>(hi) << 20);
-      std::memcpy(to + a, from + a, b - a);
+    parallel_dynamic(static_cast<int64_t>(last - first), 8, threads, [&](int, int64_t lo, int64_t hi) {
+      for (int64_t q = lo; q < hi; ++q) {
+        const Piece& pc = pieces[first + static_cast<size_t>(q)];
+        std::memcpy(to + (pc.at - off), pc.src, pc.len);
+      }
     });
-    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, to, n, cudaMemcpyHostToDevice, s);
+    first = last;
+    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, g_stage[k], n, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventRecord(done[k], s);
     used[k] = true;
   }
@@ -210,6 +314,159 @@ cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_cou
                   static_cast<void*>(dup), static_cast<void*>(bad), vals, tmp})
     if (p) cudaFreeAsync(p, s);
   if (trace.on && e == cudaSuccess) trace.mark("  csc: frees", s);
+  return e;
+}
+
+cudaError_t device_batch_csc(const BatchSetIn* sets, int32_t count, bool f64, int2* ratings, int64_t* col_ptr,
+                             int32_t* n_active_host, bool* faulty, int64_t* h2d_bytes, cudaStream_t s) {
+  *faulty = false;
+  if (count <= 0) return cudaErrorInvalidValue;
+  InitTrace trace;
+  // problem p's rows, columns and column pointers start at row_at[p], colbase[p], cpo[p]
+  std::vector<int64_t> meta(3 * (static_cast<size_t>(count) + 1), 0);
+  int64_t* row_at = meta.data();
+  int64_t* colbase = row_at + count + 1;
+  int64_t* cpo = colbase + count + 1;
+  int64_t nnz = 0;
+  int32_t max_m = 0;
+  for (int32_t p = 0; p < count; ++p) {
+    const BatchSetIn& q = sets[p];
+    if (q.m <= 0 || q.n <= 0 || q.nnz < 0) return cudaErrorInvalidValue;
+    nnz += q.nnz;
+    max_m = std::max(max_m, q.m);
+    row_at[p + 1] = row_at[p] + q.m;
+    colbase[p + 1] = colbase[p] + q.n;
+    cpo[p + 1] = cpo[p] + q.n + 1;
+  }
+  const int64_t rows = row_at[count], cols_total = colbase[count], ptrs = cpo[count];
+  if (nnz > INT_MAX || cols_total > INT_MAX || rows >= INT_MAX) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+  if (nnz == 0) {  // no ratings: every column pointer 0
+    e = cudaMemsetAsync(col_ptr, 0, static_cast<size_t>(ptrs) * sizeof(int64_t), s);
+    if (n_active_host) std::fill(n_active_host, n_active_host + count, 0);
+    return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+  }
+  const int items = static_cast<int>(nnz);
+  const int32_t n_keys = static_cast<int32_t>(cols_total);
+  int end_bit = 1;
+  while (end_bit < 32 && (static_cast<uint32_t>(n_keys - 1) >> end_bit) != 0) ++end_bit;
+  uint32_t *keys_in = nullptr, *keys_out = nullptr;
+  int2* pairs_in = nullptr;
+  int32_t *rc = nullptr, *dup = nullptr, *act = nullptr;
+  unsigned long long* bad = nullptr;
+  int64_t *cnt = nullptr, *row_ptr = nullptr, *gptr = nullptr, *meta_d = nullptr;
+  void* vals = nullptr;
+  void* tmp = nullptr;
+  const size_t vsize = f64 ? sizeof(double) : sizeof(float);
+  size_t tmp_scan = 0, tmp_sort = 0;
+  e = cub::DeviceScan::ExclusiveSum(nullptr, tmp_scan, cnt, row_ptr, static_cast<int>(rows + 1), s);
+  if (e == cudaSuccess)
+    e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_sort, keys_in, keys_out, pairs_in, ratings, items, 0, end_bit, s);
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMallocAsync(p, std::max<size_t>(bytes, 16), s);
+  };
+  alloc(reinterpret_cast<void**>(&keys_in), static_cast<size_t>(nnz) * 4);
+  alloc(reinterpret_cast<void**>(&keys_out), static_cast<size_t>(nnz) * 4);
+  alloc(reinterpret_cast<void**>(&pairs_in), static_cast<size_t>(nnz) * 8);
+  alloc(reinterpret_cast<void**>(&rc), static_cast<size_t>(rows) * 4);
+  alloc(reinterpret_cast<void**>(&cnt), (static_cast<size_t>(rows) + 1) * 8);
+  alloc(reinterpret_cast<void**>(&row_ptr), (static_cast<size_t>(rows) + 1) * 8);
+  alloc(reinterpret_cast<void**>(&gptr), (static_cast<size_t>(cols_total) + 1) * 8);
+  alloc(reinterpret_cast<void**>(&meta_d), meta.size() * 8);
+  alloc(reinterpret_cast<void**>(&act), static_cast<size_t>(count) * 4);
+  alloc(reinterpret_cast<void**>(&dup), 4);
+  alloc(reinterpret_cast<void**>(&bad), 8);
+  alloc(&vals, static_cast<size_t>(nnz) * vsize);
+  alloc(&tmp, std::max(tmp_scan, tmp_sort));
+  if (trace.on && e == cudaSuccess) trace.mark("  batch csc: allocations", s);
+  // every problem's arrays, concatenated (a set without ratings may come without arrays:
+  // its row counts are zeros)
+  std::vector<int32_t> zeros;
+  std::vector<const void*> src_c(count), src_r(count), src_v(count);
+  std::vector<size_t> len_c(count), len_r(count), len_v(count);
+  for (int32_t p = 0; p < count; ++p) {
+    const BatchSetIn& q = sets[p];
+    if (!q.row_counts && zeros.empty()) zeros.assign(static_cast<size_t>(max_m), 0);
+    src_c[p] = q.cols;
+    src_r[p] = q.row_counts ? static_cast<const void*>(q.row_counts) : static_cast<const void*>(zeros.data());
+    src_v[p] = q.vals;
+    len_c[p] = static_cast<size_t>(q.nnz) * 4;
+    len_r[p] = static_cast<size_t>(q.m) * 4;
+    len_v[p] = static_cast<size_t>(q.nnz) * vsize;
+  }
+  if (e == cudaSuccess) e = upload_staged_many(keys_in, src_c.data(), len_c.data(), count, s);
+  if (e == cudaSuccess) e = upload_staged_many(rc, src_r.data(), len_r.data(), count, s);
+  if (e == cudaSuccess) e = upload_staged_many(vals, src_v.data(), len_v.data(), count, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(meta_d, meta.data(), meta.size() * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    *h2d_bytes += static_cast<int64_t>(nnz) * (4 + static_cast<int64_t>(vsize)) + rows * 4 +
+                  static_cast<int64_t>(meta.size()) * 8;
+    const int dup_none = INT_MAX;
+    e = cudaMemcpyAsync(dup, &dup_none, 4, cudaMemcpyHostToDevice, s);
+  }
+  unsigned long long b = ~0ull;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bad, &b, 8, cudaMemcpyHostToDevice, s);
+  if (trace.on && e == cudaSuccess) trace.mark("  batch csc: copies in", s);
+  const int64_t* row_at_d = meta_d;
+  const int64_t* colbase_d = meta_d + count + 1;
+  const int64_t* cpo_d = colbase_d + count + 1;
+  if (e == cudaSuccess) {
+    counts64_kernel<<<static_cast<unsigned>((rows + 256) / 256), 256, 0, s>>>(rc, rows, cnt);
+    e = cub::DeviceScan::ExclusiveSum(tmp, tmp_scan, cnt, row_ptr, static_cast<int>(rows + 1), s);
+  }
+  if (e == cudaSuccess) {
+    batch_expand_kernel<<<static_cast<unsigned>((rows * 32 + 255) / 256), 256, 0, s>>>(
+        row_ptr, rows, row_at_d, colbase_d, count, keys_in, f64 ? static_cast<const double*>(vals) : nullptr,
+        f64 ? nullptr : static_cast<const float*>(vals), keys_in, pairs_in, bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&b, bad, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && b != ~0ull) *faulty = true;  // a column out of range: nothing is sorted
+  if (e == cudaSuccess && !*faulty)
+    e = cub::DeviceRadixSort::SortPairs(tmp, tmp_sort, keys_in, keys_out, pairs_in, ratings, items, 0, end_bit, s);
+  if (e == cudaSuccess && !*faulty) {
+    col_ptr_kernel<<<static_cast<unsigned>((nnz + 255) / 256), 256, 0, s>>>(keys_out, ratings, nnz, n_keys, gptr,
+                                                                            dup);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && !*faulty) {
+    batch_col_ptr_kernel<<<static_cast<unsigned>((ptrs + 255) / 256), 256, 0, s>>>(gptr, cpo_d, colbase_d, count,
+                                                                                   ptrs, col_ptr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && !*faulty && n_active_host) {
+    batch_active_kernel<<<static_cast<unsigned>(count), 256, 0, s>>>(gptr, colbase_d, act);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(n_active_host, act, static_cast<size_t>(count) * 4, cudaMemcpyDeviceToHost, s);
+  }
+  int32_t d = INT_MAX;
+  if (e == cudaSuccess && !*faulty) e = cudaMemcpyAsync(&d, dup, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && d != INT_MAX) *faulty = true;
+  if (trace.on && e == cudaSuccess) trace.mark("  batch csc: sort and offsets", s);
+  for (void* p : {static_cast<void*>(keys_in), static_cast<void*>(keys_out), static_cast<void*>(pairs_in),
+                  static_cast<void*>(rc), static_cast<void*>(cnt), static_cast<void*>(row_ptr),
+                  static_cast<void*>(gptr), static_cast<void*>(meta_d), static_cast<void*>(act),
+                  static_cast<void*>(dup), static_cast<void*>(bad), vals, tmp})
+    if (p) cudaFreeAsync(p, s);
+  return e;
+}
+
+cudaError_t device_batch_segs(const int2* ratings, const int64_t* col_ptr, const BatchSegIn* big_host, int32_t n_big,
+                              const int32_t* rs, int32_t R, int64_t* seg, cudaStream_t s) {
+  if (n_big <= 0) return cudaSuccess;
+  BatchSegIn* big = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&big), static_cast<size_t>(n_big) * sizeof(BatchSegIn), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(big, big_host, static_cast<size_t>(n_big) * sizeof(BatchSegIn), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    batch_segs_kernel<<<static_cast<unsigned>(n_big), 256, 0, s>>>(ratings, col_ptr, big, rs, R, seg);
+    e = cudaGetLastError();
+  }
+  if (big) cudaFreeAsync(big, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e;
 }
 

@@ -194,8 +194,38 @@ void device_layout_release(DeviceLayout* t, cudaStream_t s);
 // copies are done.  Copies straight from pageable memory ran ~30x slower when the host
 // had been under heavy allocation beforehand.
 cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s);
+// The same for `count` host arrays copied one after another into dst.
+cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t* bytes, size_t count,
+                               cudaStream_t s);
 // The rows of a device CSC's ratings (nnz entries) copied to host memory.
 cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s);
+// One rating set of one problem of a batch, row-major as for device_csc (row counts
+// already checked to add up to nnz); the arrays may be NULL when nnz is 0.
+struct BatchSetIn {
+  int64_t nnz;
+  int32_t m, n;
+  const int32_t* row_counts;
+  const int32_t* cols;
+  const void* vals;  // double or float, the same for every problem
+};
+// The CSCs of `count` problems' sets built together on the device: one stable radix sort
+// of all entries by (problem, column), so ratings hold problem after problem, each in
+// column order with rows ascending inside a column ({row, value bits}, sum of nnz
+// entries), and col_ptr problem after problem n + 1 offsets into ratings (sum of n + 1
+// entries); both caller-allocated.  n_active_host (or NULL) receives each problem's
+// columns with ratings.  *faulty is set, with nothing else guaranteed, when a column index
+// is out of range or a (row, column) cell repeats.  The sum of nnz is at most INT_MAX,
+// the sum of n below 2^32.
+cudaError_t device_batch_csc(const BatchSetIn* sets, int32_t count, bool f64, int2* ratings, int64_t* col_ptr,
+                             int32_t* n_active_host, bool* faulty, int64_t* h2d_bytes, cudaStream_t s);
+// A large batched problem's visit bounds: for each of its n columns, R + 1 offsets into
+// ratings, the first rating of the column whose row is at least rs[w] (w = 0..R).
+struct BatchSegIn {
+  int64_t col_off, seg_off;  // the problem's column pointers in col_ptr; its bounds in seg
+  int32_t n, rs_off;         // columns; its R + 1 row-block starts in rs
+};
+cudaError_t device_batch_segs(const int2* ratings, const int64_t* col_ptr, const BatchSegIn* big_host, int32_t n_big,
+                              const int32_t* rs, int32_t R, int64_t* seg, cudaStream_t s);
 cudaError_t launch_build_segx(const int4* segs, const int2* ratings, int64_t nseg, int4* segx, cudaStream_t s);
 cudaError_t async2_occupancy(int bf16, int nv, int warps, int kpad, int cta_heavy, int* blocks_per_sm);
 cudaError_t launch_replay(const ReplayArgs& a, cudaStream_t s);

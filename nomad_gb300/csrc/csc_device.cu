@@ -8,9 +8,13 @@
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstring>
+#include <memory>
 #include <mutex>
+#include <thread>
+#include <vector>
 
 #include "common.h"
 #include "launch.h"
@@ -174,37 +178,56 @@ cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t*
     }
   }
   if (total == 0) return cudaSuccess;
+  // window w: bytes [w S, (w + 1) S) of the concatenation (S = kStageBytes), pieces
+  // [wfirst[w], wfirst[w + 1]), staged in buffer w % 2
+  const size_t nwin = (total + kStageBytes - 1) / kStageBytes;
+  std::vector<size_t> wfirst(nwin + 1, pieces.size());
+  for (size_t q = pieces.size(); q-- > 0;) wfirst[pieces[q].at / kStageBytes] = q;
   std::lock_guard<std::mutex> lock(g_stage_mu);
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 2 && e == cudaSuccess; ++i)
     if (!g_stage[i]) e = cudaHostAlloc(reinterpret_cast<void**>(&g_stage[i]), kStageBytes, cudaHostAllocPortable);
   cudaEvent_t done[2] = {nullptr, nullptr};
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
-  const int threads = host_threads();
-  bool used[2] = {false, false};
-  size_t first = 0;  // the window's first piece
-  for (size_t off = 0, k = 0; off < total && e == cudaSuccess; off += kStageBytes, k ^= 1) {
-    const size_t n = std::min(kStageBytes, total - off);
-    size_t last = first;
-    while (last < pieces.size() && pieces[last].at < off + n) ++last;
-    if (used[k]) e = cudaEventSynchronize(done[k]);  // the copy out of this buffer is done
-    if (e != cudaSuccess) break;
-    char* to = g_stage[k];
-    parallel_dynamic(static_cast<int64_t>(last - first), 8, threads, [&](int, int64_t lo, int64_t hi) {
-      for (int64_t q = lo; q < hi; ++q) {
-        const Piece& pc = pieces[first + static_cast<size_t>(q)];
-        std::memcpy(to + (pc.at - off), pc.src, pc.len);
+  if (e == cudaSuccess) {
+    // T host threads, started once, fill window w when its buffer is free (w <= ready);
+    // this thread queues each window's copy once every filler is through it (filled[w] =
+    // T), then waits for the previous window's copy, which frees that buffer for w + 1.
+    const int T = static_cast<int>(std::min<size_t>(static_cast<size_t>(std::max(1, host_threads() - 1)), pieces.size()));
+    std::unique_ptr<std::atomic<int>[]> filled(new std::atomic<int>[nwin]);
+    for (size_t w = 0; w < nwin; ++w) filled[w].store(0);
+    std::atomic<int64_t> ready{1};
+    std::atomic<bool> stop{false};
+    auto fill = [&](int t) {
+      for (size_t w = 0; w < nwin; ++w) {
+        while (ready.load(std::memory_order_acquire) < static_cast<int64_t>(w) && !stop.load())
+          std::this_thread::yield();
+        if (!stop.load()) {
+          char* to = g_stage[w & 1];
+          for (size_t q = wfirst[w] + static_cast<size_t>(t); q < wfirst[w + 1]; q += static_cast<size_t>(T))
+            std::memcpy(to + (pieces[q].at - w * kStageBytes), pieces[q].src, pieces[q].len);
+        }
+        filled[w].fetch_add(1, std::memory_order_release);
       }
-    });
-    first = last;
-    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, g_stage[k], n, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaEventRecord(done[k], s);
-    used[k] = true;
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(static_cast<size_t>(T));
+    for (int t = 0; t < T; ++t) pool.emplace_back(fill, t);
+    for (size_t w = 0; w < nwin && e == cudaSuccess; ++w) {
+      while (filled[w].load(std::memory_order_acquire) < T) std::this_thread::yield();
+      const size_t n = std::min(kStageBytes, total - w * kStageBytes);
+      e = cudaMemcpyAsync(static_cast<char*>(dst) + w * kStageBytes, g_stage[w & 1], n, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaEventRecord(done[w & 1], s);
+      if (e == cudaSuccess && w >= 1) e = cudaEventSynchronize(done[(w - 1) & 1]);
+      ready.store(static_cast<int64_t>(w) + 1, std::memory_order_release);
+    }
+    if (e != cudaSuccess) stop.store(true);
+    for (auto& th : pool) th.join();
   }
   // the buffers are reused by the next upload: its copies into them wait for these
   for (int i = 0; i < 2; ++i)
     if (done[i]) {
-      if (used[i] && e == cudaSuccess) e = cudaEventSynchronize(done[i]);
+      if (e == cudaSuccess) e = cudaEventSynchronize(done[i]);
       cudaEventDestroy(done[i]);
     }
   return e;

@@ -123,6 +123,15 @@ int ensure_graph(nomad_gpu_batch* b) {
   return NOMAD_OK;
 }
 
+// A temporary device buffer, freed when it goes out of scope.
+struct DevTemp {
+  void* p = nullptr;
+  cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, std::max<size_t>(bytes, 16)); }
+  ~DevTemp() {
+    if (p) cudaFree(p);
+  }
+};
+
 // Whether the device build takes every problem's sets: each row-major or empty, one value
 // type throughout (*f64), the totals within its limits.
 bool device_batch_ok(const nomad_gpu_batch_problem* P, int32_t count, bool* f64) {
@@ -457,56 +466,123 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   }
 
   trace.mark("uploads", b->stream);
-  // ---- factors: given, or the reference init of each problem.  Problems go in groups
-  // of at most kStage floats: the group's dense fp32 rows are generated in parallel on the
-  // host, copied once, and converted to the padded storage per problem on the device.
-  constexpr int64_t kStage = int64_t(1) << 26;  // 256 MB of fp32
-  float* stage = nullptr;
-  int64_t stage_len = 0;
-  for (int32_t i = 0; i < count; ++i)
-    stage_len = std::max<int64_t>(stage_len, static_cast<int64_t>(P[i].m + P[i].n) * P[i].dim);
-  stage_len = std::max(stage_len, std::min<int64_t>(kStage, (w_off + h_off)));
-  RC(dalloc(b, &stage, static_cast<size_t>(stage_len)));
-  std::vector<float, nomad::NoInitAllocator<float>> host(static_cast<size_t>(stage_len));
-  for (int32_t g0 = 0; g0 < count;) {
-    // the group [g0, g1): consecutive problems whose rows fit the staging buffer
-    std::vector<int64_t> at;
-    int64_t used = 0;
-    int32_t g1 = g0;
-    while (g1 < count) {
-      const int64_t need = static_cast<int64_t>(P[g1].m + P[g1].n) * P[g1].dim;
-      if (g1 > g0 && used + need > stage_len) break;
-      at.push_back(used);
-      used += need;
-      ++g1;
-    }
-    nomad::parallel_dynamic(g1 - g0, 1, threads, [&](int, int64_t lo, int64_t hi) {
-      for (int64_t t = lo; t < hi; ++t) {
-        const nomad_gpu_batch_problem& q = P[g0 + t];
-        float* Wh = host.data() + at[t];
-        float* Hh = Wh + static_cast<int64_t>(q.m) * q.dim;
-        if (q.W0)
-          std::copy(q.W0, q.W0 + static_cast<int64_t>(q.m) * q.dim, Wh);
-        else
-          nomad_reference_init(q.m, 0, q.dim, p.seed, std::max(p.init_parts, 1), Wh, nullptr);
-        if (q.H0)
-          std::copy(q.H0, q.H0 + static_cast<int64_t>(q.n) * q.dim, Hh);
-        else
-          nomad_reference_init(0, q.n, q.dim, p.seed, std::max(p.init_parts, 1), nullptr, Hh);
-      }
-    });
-    CK(cudaMemcpyAsync(stage, host.data(), static_cast<size_t>(used) * sizeof(float), cudaMemcpyHostToDevice,
-                       b->stream));
-    for (int32_t i = g0; i < g1; ++i) {
+  // ---- factors.  Rows not given take the reference init (nomad_reference_init): every
+  // such problem draws from the same streams -- W's row block t from seed + t + 1, H from
+  // seed + 139 -- so each stream is drawn here once, as far as the longest problem needs,
+  // and a kernel scales and stores every problem's rows.  Given rows are copied in
+  // through the pinned staging buffers in groups of at most kStage floats and converted
+  // to the padded storage on the device.
+  {
+    const int32_t parts = std::max(p.init_parts, 1);
+    std::vector<int64_t> lw(parts, 0), c_off(static_cast<size_t>(parts) + 1, 0);
+    int64_t lh = 0;
+    std::vector<nomad::BatchInitIn> init_in(2 * static_cast<size_t>(count));  // W sides, then H sides
+    std::vector<int64_t> offs(2 * (static_cast<size_t>(count) + 1));          // element offsets, likewise
+    bool any = false;
+    for (int32_t i = 0; i < count; ++i) {
       const nomad_gpu_batch_problem& q = P[i];
       const nomad::BatchProblem& pb = b->probs[i];
-      const float* src = stage + at[i - g0];
-      CK(nomad::launch_f32_to_store(src, W + pb.w_off * b->esz, q.m, q.dim, pb.kpad, bf16, b->stream));
-      CK(nomad::launch_f32_to_store(src + static_cast<int64_t>(q.m) * q.dim, H + pb.h_off * b->esz, q.n, q.dim,
-                                    pb.kpad, bf16, b->stream));
+      const int32_t rpp = q.m / parts + (q.m % parts > 0 ? 1 : 0);
+      const double bound = 1.0 / std::sqrt(q.dim);
+      init_in[i] = nomad::BatchInitIn{q.m, q.dim, pb.kpad, rpp, q.W0 ? 0 : 1, 0, bound};
+      init_in[count + i] = nomad::BatchInitIn{q.n, q.dim, pb.kpad, q.n, q.H0 ? 0 : 1, 0, bound};
+      offs[i] = pb.w_off;
+      offs[count + 1 + i] = pb.h_off;
+      if (!q.W0)
+        for (int32_t t = 0; t < parts; ++t) {
+          const int64_t lo = std::min<int64_t>(int64_t(rpp) * t, q.m), hi = std::min<int64_t>(int64_t(rpp) * (t + 1), q.m);
+          lw[t] = std::max(lw[t], (hi - lo) * q.dim);
+        }
+      if (!q.H0) lh = std::max<int64_t>(lh, int64_t(q.n) * q.dim);
+      any = any || !q.W0 || !q.H0;
     }
-    CK(cudaStreamSynchronize(b->stream));  // the host and device staging buffers are reused
-    g0 = g1;
+    offs[count] = w_off;
+    offs[2 * static_cast<size_t>(count) + 1] = h_off;
+    if (any) {
+      for (int32_t t = 0; t < parts; ++t) c_off[t + 1] = c_off[t] + lw[t];
+      // the canonical values: W's row-block streams, then H's stream at c_off[parts]
+      std::vector<double> c(static_cast<size_t>(c_off[parts] + lh));
+      nomad::parallel_dynamic(parts + 1, 1, threads, [&](int, int64_t lo, int64_t hi) {
+        for (int64_t t = lo; t < hi; ++t) {
+          if (t < parts) nomad::reference_canonical(p.seed + static_cast<uint64_t>(t) + 1, lw[t], c.data() + c_off[t]);
+          else nomad::reference_canonical(p.seed + 139, lh, c.data() + c_off[parts]);
+        }
+      });
+      DevTemp c_d, coff_d, in_d, offs_d;
+      CK(c_d.alloc(c.size() * sizeof(double)));
+      CK(coff_d.alloc(c_off.size() * sizeof(int64_t)));
+      CK(in_d.alloc(init_in.size() * sizeof(nomad::BatchInitIn)));
+      CK(offs_d.alloc(offs.size() * sizeof(int64_t)));
+      CK(nomad::upload_staged(c_d.p, c.data(), c.size() * sizeof(double), b->stream));
+      CK(cudaMemcpyAsync(coff_d.p, c_off.data(), c_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+      CK(cudaMemcpyAsync(in_d.p, init_in.data(), init_in.size() * sizeof(nomad::BatchInitIn), cudaMemcpyHostToDevice,
+                         b->stream));
+      CK(cudaMemcpyAsync(offs_d.p, offs.data(), offs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+      const auto* in = static_cast<const nomad::BatchInitIn*>(in_d.p);
+      const auto* of = static_cast<const int64_t*>(offs_d.p);
+      const auto* cd = static_cast<const double*>(c_d.p);
+      const auto* co = static_cast<const int64_t*>(coff_d.p);
+      CK(nomad::launch_batch_ref_init(in, of, count, w_off, cd, co, W, bf16, b->stream));
+      CK(nomad::launch_batch_ref_init(in + count, of + count + 1, count, h_off, cd, co + parts, H, bf16, b->stream));
+      CK(cudaStreamSynchronize(b->stream));
+    }
+    trace.mark("factors: reference init");
+    constexpr int64_t kStage = int64_t(1) << 26;  // 256 MB of fp32
+    std::vector<int32_t> given;
+    int64_t stage_len = 0, all = 0;
+    auto need = [&](int32_t i) {
+      return (P[i].W0 ? int64_t(P[i].m) * P[i].dim : 0) + (P[i].H0 ? int64_t(P[i].n) * P[i].dim : 0);
+    };
+    for (int32_t i = 0; i < count; ++i)
+      if (P[i].W0 || P[i].H0) {
+        given.push_back(i);
+        stage_len = std::max(stage_len, need(i));
+        all += need(i);
+      }
+    if (!given.empty()) {
+      stage_len = std::max(stage_len, std::min(kStage, all));
+      DevTemp stage_d;
+      CK(stage_d.alloc(static_cast<size_t>(stage_len) * sizeof(float)));
+      float* stage = static_cast<float*>(stage_d.p);
+      for (size_t g0 = 0; g0 < given.size();) {
+        // the group [g0, g1): consecutive problems whose given rows fit the staging buffer
+        std::vector<const void*> srcs;
+        std::vector<size_t> lens;
+        std::vector<int64_t> at;
+        int64_t used = 0;
+        size_t g1 = g0;
+        while (g1 < given.size()) {
+          const nomad_gpu_batch_problem& q = P[given[g1]];
+          if (g1 > g0 && used + need(given[g1]) > stage_len) break;
+          at.push_back(used);
+          if (q.W0) {
+            srcs.push_back(q.W0);
+            lens.push_back(static_cast<size_t>(q.m) * q.dim * sizeof(float));
+          }
+          if (q.H0) {
+            srcs.push_back(q.H0);
+            lens.push_back(static_cast<size_t>(q.n) * q.dim * sizeof(float));
+          }
+          used += need(given[g1]);
+          ++g1;
+        }
+        // conversions of the previous group are ahead of this copy on the stream
+        CK(nomad::upload_staged_many(stage, srcs.data(), lens.data(), srcs.size(), b->stream));
+        for (size_t g = g0; g < g1; ++g) {
+          const nomad_gpu_batch_problem& q = P[given[g]];
+          const nomad::BatchProblem& pb = b->probs[given[g]];
+          const float* src = stage + at[g - g0];
+          if (q.W0) {
+            CK(nomad::launch_f32_to_store(src, W + pb.w_off * b->esz, q.m, q.dim, pb.kpad, bf16, b->stream));
+            src += static_cast<int64_t>(q.m) * q.dim;
+          }
+          if (q.H0)
+            CK(nomad::launch_f32_to_store(src, H + pb.h_off * b->esz, q.n, q.dim, pb.kpad, bf16, b->stream));
+        }
+        g0 = g1;
+      }
+      CK(cudaStreamSynchronize(b->stream));
+    }
   }
 
   trace.mark("factors");

@@ -56,6 +56,11 @@ struct SplitMix64 {
   double normal();  // Box-Muller
 };
 
+// The first `count` draws of mt19937_64(stream_seed) as generate_canonical<double>
+// values in [0, 1): the reference init's value i of that stream is float(c[i] * b + 0.0)
+// for b = 1/sqrt(dim) (nomad_reference_init draws the same values).
+void reference_canonical(uint64_t stream_seed, int64_t count, double* dst);
+
 // Stream key for entity `id` of purpose `tag` under `seed`.
 inline uint64_t stream_key(uint64_t seed, uint64_t tag, uint64_t id) {
   return SplitMix64::mix(seed ^ SplitMix64::mix(tag * 0x632BE59BD9B4E019ULL + id));

@@ -262,6 +262,21 @@ class Mt64Uniform {
     mt_[0] = seed;
     for (int i = 1; i < kN; ++i) mt_[i] = 6364136223846793005ULL * (mt_[i - 1] ^ (mt_[i - 1] >> 62)) + static_cast<uint64_t>(i);
   }
+  // the canonical values x / 2^64 (below 1) themselves
+  void fill_canonical(double* dst, int64_t count) {
+    const double below_one = std::nextafter(1.0, 0.0);
+    while (count > 0) {
+      if (pos_ == kN) twist();
+      const int take = static_cast<int>(std::min<int64_t>(count, kN - pos_));
+      for (int k = 0; k < take; ++k) {
+        const double c = static_cast<double>(out_[pos_ + k]) * 0x1p-64;
+        dst[k] = c >= 1.0 ? below_one : c;
+      }
+      pos_ += take;
+      dst += take;
+      count -= take;
+    }
+  }
   void fill(float* dst, int64_t count, double b) {
     const double below_one = std::nextafter(1.0, 0.0);
     while (count > 0) {
@@ -306,6 +321,14 @@ class Mt64Uniform {
 };
 
 }  // namespace
+
+extern "C++" {
+namespace nomad {
+void reference_canonical(uint64_t stream_seed, int64_t count, double* dst) {
+  Mt64Uniform(stream_seed).fill_canonical(dst, count);
+}
+}  // namespace nomad
+}
 
 // nb_main.cpp:450-455 (rows of part t from mt19937_64(seed + rank*131 + t + 1)) and
 // nb_main.cpp:71-92 (every column's values from mt19937_64(seed + rank*131 + 139)),

@@ -200,6 +200,39 @@ __global__ void f32_to_store_kernel(const float* __restrict__ src, Store* __rest
       reinterpret_cast<__nv_bfloat16*>(dst)[i] = __float2bfloat16_rn(v);
   }
 }
+// One thread per element of a side's concatenated rows (grid-stride); the problem of an
+// element by binary search over the side's offsets.
+template <typename Store>
+__global__ void batch_ref_init_kernel(const nomad::BatchInitIn* __restrict__ probs, const int64_t* __restrict__ off,
+                                      int32_t count, int64_t total, const double* __restrict__ c,
+                                      const int64_t* __restrict__ c_off, Store* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int32_t lo = 0, hi = count;
+    while (hi - lo > 1) {
+      const int32_t mid = (lo + hi) >> 1;
+      if (off[mid] <= i) lo = mid;
+      else hi = mid;
+    }
+    const nomad::BatchInitIn q = probs[lo];
+    if (!q.init) continue;
+    const int64_t local = i - off[lo];
+    const int64_t r = local / q.kpad;
+    const int k = static_cast<int>(local - r * q.kpad);
+    float v = 0.f;
+    if (k < q.dim) {
+      const int64_t t = r / q.rpp;
+      // uniform_real_distribution<double>(0, b): canonical value times b (plus 0.0, which
+      // leaves a non-negative product as it is), narrowed to float
+      v = __double2float_rn(__dmul_rn(c[c_off[t] + (r - t * q.rpp) * q.dim + k], q.b));
+    }
+    if (sizeof(Store) == 4)
+      reinterpret_cast<float*>(dst)[i] = v;
+    else
+      reinterpret_cast<__nv_bfloat16*>(dst)[i] = __float2bfloat16_rn(v);
+  }
+}
+
 template <typename Store>
 __global__ void store_to_f32_kernel(const Store* __restrict__ src, float* __restrict__ dst,
                                     int64_t rows, int dim, int kpad) {
@@ -297,6 +330,18 @@ cudaError_t launch_f32_to_store(const float* src, void* dst, int64_t rows, int32
   else
     f32_to_store_kernel<float><<<grid_for(rows * kpad), 256, 0, s>>>(src, static_cast<float*>(dst),
                                                                      rows, dim, kpad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_ref_init(const BatchInitIn* probs, const int64_t* off, int32_t count, int64_t total,
+                                  const double* c, const int64_t* c_off, void* dst, int bf16, cudaStream_t s) {
+  if (total <= 0 || count <= 0) return cudaSuccess;
+  if (bf16)
+    batch_ref_init_kernel<__nv_bfloat16><<<grid_for(total), 256, 0, s>>>(probs, off, count, total, c, c_off,
+                                                                         static_cast<__nv_bfloat16*>(dst));
+  else
+    batch_ref_init_kernel<float><<<grid_for(total), 256, 0, s>>>(probs, off, count, total, c, c_off,
+                                                                 static_cast<float*>(dst));
   return cudaGetLastError();
 }
 

@@ -253,6 +253,21 @@ cudaError_t launch_f32_to_store(const float* src, void* dst, int64_t rows, int32
                                 int32_t kpad, int bf16, cudaStream_t s);
 cudaError_t launch_store_to_f32(const void* src, float* dst, int64_t rows, int32_t dim,
                                 int32_t kpad, int bf16, cudaStream_t s);
+// The reference init of batched problems' rows on the device.  Every problem draws from
+// the same streams (W's row block t from one stream, H from another), so the streams'
+// canonical values are drawn once on the host as far as the longest problem needs and
+// uploaded; value k of row r of W is float(c[t][(r - t rpp) dim + k] b + 0.0), t = r /
+// rpp, and of H float(ch[r dim + k] b + 0.0), padding columns 0, stored as fp32 or bf16
+// (round to nearest) at the problem's offsets.  Problems whose `side` flag is 0 are
+// left alone.  off[p] are the problems' element offsets in the side's concatenation
+// (count + 1 entries, increasing).
+struct BatchInitIn {
+  int32_t rows, dim, kpad, rpp;  // rows of the side; rpp: rows per row block (W), else rows
+  int32_t init, pad;             // 1: draw this side's rows
+  double b;                      // 1 / sqrt(dim)
+};
+cudaError_t launch_batch_ref_init(const BatchInitIn* probs, const int64_t* off, int32_t count, int64_t total,
+                                  const double* c, const int64_t* c_off, void* dst, int bf16, cudaStream_t s);
 cudaError_t launch_empty_queues(int32_t* qnext, int32_t* qtail, int32_t n, int32_t P,
                                 cudaStream_t s);
 

@@ -102,3 +102,31 @@ def test_batch_rmse_matches_single_problem_evaluation(ng, gpu_ok):
         with ng.Nomad(train, test, W0=W, H0=H, dim=dim, mode="replay") as nm:
             r_tr, r_te = nm.rmse()
         assert abs(a - r_tr) <= 1e-5 * r_tr and abs(c - r_te) <= 1e-5 * r_te
+
+
+def bf16_rn(x):
+    """float32 values rounded to the nearest bfloat16 (ties to even), as float32."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return (((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16).astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("parts", [1, 3])
+def test_batch_reference_init_on_device(ng, gpu_ok, precision, parts):
+    """Rows not given take the reference init, drawn once per stream on the host and
+    expanded on the device: every problem's rows equal nomad_reference_init's (rounded to
+    bf16 for bf16 storage); given rows are kept as given."""
+    probs = small_batch(ng, count=6)
+    batch = []
+    for i, (train, test, dim, W0, H0) in enumerate(probs):
+        W1, H1 = W0 + 0.25, H0 + 0.5  # given rows that differ from the init
+        batch.append((train, test, dim, W1 if i == 1 else None, H1 if i in (2, 4) else None))
+    seed = 777
+    with ng.Batch(batch, lrate=LR, drate=DR, reg=REG, precision=precision, seed=seed, init_parts=parts) as b:
+        got = [b.factors(i) for i in range(len(batch))]
+    conv = bf16_rn if precision == "bf16" else (lambda x: x)
+    for (train, test, dim, Wg, Hg), (W, H) in zip(batch, got):
+        Wr, Hr = ng.reference_init(train.m, train.n, dim, seed, parts)
+        assert np.array_equal(W, conv(Wg if Wg is not None else Wr)), (train.m, dim)
+        assert np.array_equal(H, conv(Hg if Hg is not None else Hr)), (train.n, dim)

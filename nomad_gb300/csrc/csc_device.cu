@@ -34,17 +34,13 @@ __global__ void check_cols_kernel(const uint32_t* cols, int64_t nnz, int32_t n, 
   if (i < nnz && cols[i] >= static_cast<uint32_t>(n)) atomicMin(bad, static_cast<unsigned long long>(i));
 }
 
-// One warp per row: every entry of row r becomes {r, value as fp32}.
-__global__ void expand_rows_kernel(const int64_t* row_ptr, int32_t m, const double* v64, const float* v32,
-                                   int2* pairs) {
+// One warp per row: every entry of row r becomes {r, value bits}.
+__global__ void expand_rows_kernel(const int64_t* row_ptr, int32_t m, const float* vals, int2* pairs) {
   const int64_t r = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= m) return;
   const int64_t b = row_ptr[r], e = row_ptr[r + 1];
-  for (int64_t i = b + lane; i < e; i += 32) {
-    const float v = v64 ? static_cast<float>(v64[i]) : v32[i];
-    pairs[i] = make_int2(static_cast<int32_t>(r), __float_as_int(v));
-  }
+  for (int64_t i = b + lane; i < e; i += 32) pairs[i] = make_int2(static_cast<int32_t>(r), __float_as_int(vals[i]));
 }
 
 // col_ptr from the sorted column keys (each column's first entry, empty columns included)
@@ -80,10 +76,10 @@ __device__ __forceinline__ int32_t owner_of(const int64_t* at, int32_t count, in
 
 // Batched sets, one warp per row of the concatenated row-major entries: row r of problem
 // p gives each of its entries the key colbase[p] + column and the pair {local row, value
-// as fp32}; the first entry with a column outside [0, n_p) goes to *bad.
+// bits}; the first entry with a column outside [0, n_p) goes to *bad.
 __global__ void batch_expand_kernel(const int64_t* row_ptr, int64_t rows, const int64_t* row_at,
-                                    const int64_t* colbase, int32_t count, const uint32_t* cols, const double* v64,
-                                    const float* v32, uint32_t* keys, int2* pairs, unsigned long long* bad) {
+                                    const int64_t* colbase, int32_t count, const uint32_t* cols, const float* vals,
+                                    uint32_t* keys, int2* pairs, unsigned long long* bad) {
   const int64_t r = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= rows) return;
@@ -96,8 +92,7 @@ __global__ void batch_expand_kernel(const int64_t* row_ptr, int64_t rows, const 
     const uint32_t c = cols[i];
     if (c >= n) atomicMin(bad, static_cast<unsigned long long>(i));
     keys[i] = c < n ? static_cast<uint32_t>(base + c) : 0u;
-    const float v = v64 ? static_cast<float>(v64[i]) : v32[i];
-    pairs[i] = make_int2(local, __float_as_int(v));
+    pairs[i] = make_int2(local, __float_as_int(vals[i]));
   }
 }
 
@@ -154,13 +149,14 @@ char* g_stage[2] = {nullptr, nullptr};
 
 namespace nomad {
 
-cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
-  return upload_staged_many(dst, &src, &bytes, 1, s);
-}
+namespace {
 
-cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t* bytes, size_t count,
-                               cudaStream_t s) {
-  // pieces of at most 1 MB, none across a staging window
+// The staged copy of `count` host arrays, one after another, into dst: bytes[i] bytes of
+// destination each, copied as they are or (narrow) narrowed from twice as many bytes of
+// doubles to floats, round to nearest.
+cudaError_t staged(void* dst, const void* const* srcs, const size_t* bytes, size_t count, bool narrow,
+                   cudaStream_t s) {
+  // pieces of at most 1 MB of destination, none across a staging window
   struct Piece {
     const char* src;
     size_t at, len;
@@ -172,7 +168,7 @@ cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t*
     for (size_t left = bytes[i]; left > 0;) {
       const size_t len = std::min({left, kStageBytes - total % kStageBytes, size_t{1} << 20});
       pieces.push_back(Piece{p, total, len});
-      p += len;
+      p += narrow ? 2 * len : len;
       total += len;
       left -= len;
     }
@@ -204,8 +200,16 @@ cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t*
           std::this_thread::yield();
         if (!stop.load()) {
           char* to = g_stage[w & 1];
-          for (size_t q = wfirst[w] + static_cast<size_t>(t); q < wfirst[w + 1]; q += static_cast<size_t>(T))
-            std::memcpy(to + (pieces[q].at - w * kStageBytes), pieces[q].src, pieces[q].len);
+          for (size_t q = wfirst[w] + static_cast<size_t>(t); q < wfirst[w + 1]; q += static_cast<size_t>(T)) {
+            char* at = to + (pieces[q].at - w * kStageBytes);
+            if (!narrow) {
+              std::memcpy(at, pieces[q].src, pieces[q].len);
+              continue;
+            }
+            const double* from = reinterpret_cast<const double*>(pieces[q].src);
+            float* out = reinterpret_cast<float*>(at);
+            for (size_t k = 0; k < pieces[q].len / sizeof(float); ++k) out[k] = static_cast<float>(from[k]);
+          }
         }
         filled[w].fetch_add(1, std::memory_order_release);
       }
@@ -231,6 +235,24 @@ cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t*
       cudaEventDestroy(done[i]);
     }
   return e;
+}
+
+}  // namespace
+
+cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  return staged(dst, &src, &bytes, 1, false, s);
+}
+
+cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t* bytes, size_t count,
+                               cudaStream_t s) {
+  return staged(dst, srcs, bytes, count, false, s);
+}
+
+cudaError_t upload_staged_narrow(float* dst, const double* const* srcs, const size_t* counts, size_t count,
+                                 cudaStream_t s) {
+  std::vector<size_t> bytes(count);
+  for (size_t i = 0; i < count; ++i) bytes[i] = counts[i] * sizeof(float);
+  return staged(dst, reinterpret_cast<const void* const*>(srcs), bytes.data(), count, true, s);
 }
 
 cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s) {
@@ -266,7 +288,7 @@ cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_cou
   int64_t *cnt = nullptr, *row_ptr = nullptr;
   void* vals = nullptr;
   void* tmp = nullptr;
-  const size_t vbytes = static_cast<size_t>(nnz) * (v64 ? sizeof(double) : sizeof(float));
+  const size_t vbytes = static_cast<size_t>(nnz) * sizeof(float);  // fp64 values narrowed as they are staged
   size_t tmp_scan = 0, tmp_sort = 0;
   cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, tmp_scan, cnt, row_ptr, m + 1, s);
   if (e == cudaSuccess)
@@ -289,8 +311,10 @@ cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_cou
   // the caller's arrays are pageable memory of any mapping: staged through pinned buffers
   if (e == cudaSuccess) e = upload_staged(keys_in, cols, static_cast<size_t>(nnz) * 4, s);
   if (e == cudaSuccess) e = upload_staged(rc, row_counts, static_cast<size_t>(m) * 4, s);
-  if (e == cudaSuccess)
-    e = upload_staged(vals, v64 ? static_cast<const void*>(v64) : static_cast<const void*>(v32), vbytes, s);
+  if (e == cudaSuccess) {
+    const size_t n_vals = static_cast<size_t>(nnz);
+    e = v64 ? upload_staged_narrow(static_cast<float*>(vals), &v64, &n_vals, 1, s) : upload_staged(vals, v32, vbytes, s);
+  }
   if (e == cudaSuccess) {
     *h2d_bytes += static_cast<int64_t>(nnz) * 4 + static_cast<int64_t>(m) * 4 + static_cast<int64_t>(vbytes);
     const int dup_none = INT_MAX;
@@ -317,8 +341,7 @@ cudaError_t device_csc(int64_t nnz, int32_t m, int32_t n, const int32_t* row_cou
   if (e == cudaSuccess) {
     const int64_t threads = static_cast<int64_t>(m) * 32;
     expand_rows_kernel<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, s>>>(
-        row_ptr, m, v64 ? static_cast<const double*>(vals) : nullptr, v64 ? nullptr : static_cast<const float*>(vals),
-        pairs_in);
+        row_ptr, m, static_cast<const float*>(vals), pairs_in);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)
@@ -380,7 +403,7 @@ cudaError_t device_batch_csc(const BatchSetIn* sets, int32_t count, bool f64, in
   int64_t *cnt = nullptr, *row_ptr = nullptr, *gptr = nullptr, *meta_d = nullptr;
   void* vals = nullptr;
   void* tmp = nullptr;
-  const size_t vsize = f64 ? sizeof(double) : sizeof(float);
+  const size_t vsize = sizeof(float);  // fp64 values narrowed as they are staged
   size_t tmp_scan = 0, tmp_sort = 0;
   e = cub::DeviceScan::ExclusiveSum(nullptr, tmp_scan, cnt, row_ptr, static_cast<int>(rows + 1), s);
   if (e == cudaSuccess)
@@ -415,11 +438,14 @@ cudaError_t device_batch_csc(const BatchSetIn* sets, int32_t count, bool f64, in
     src_v[p] = q.vals;
     len_c[p] = static_cast<size_t>(q.nnz) * 4;
     len_r[p] = static_cast<size_t>(q.m) * 4;
-    len_v[p] = static_cast<size_t>(q.nnz) * vsize;
+    len_v[p] = static_cast<size_t>(q.nnz) * (f64 ? 1 : vsize);  // values (fp64) or bytes (fp32)
   }
   if (e == cudaSuccess) e = upload_staged_many(keys_in, src_c.data(), len_c.data(), count, s);
   if (e == cudaSuccess) e = upload_staged_many(rc, src_r.data(), len_r.data(), count, s);
-  if (e == cudaSuccess) e = upload_staged_many(vals, src_v.data(), len_v.data(), count, s);
+  if (e == cudaSuccess)
+    e = f64 ? upload_staged_narrow(static_cast<float*>(vals), reinterpret_cast<const double* const*>(src_v.data()),
+                                   len_v.data(), count, s)
+            : upload_staged_many(vals, src_v.data(), len_v.data(), count, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(meta_d, meta.data(), meta.size() * 8, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     *h2d_bytes += static_cast<int64_t>(nnz) * (4 + static_cast<int64_t>(vsize)) + rows * 4 +
@@ -439,8 +465,7 @@ cudaError_t device_batch_csc(const BatchSetIn* sets, int32_t count, bool f64, in
   }
   if (e == cudaSuccess) {
     batch_expand_kernel<<<static_cast<unsigned>((rows * 32 + 255) / 256), 256, 0, s>>>(
-        row_ptr, rows, row_at_d, colbase_d, count, keys_in, f64 ? static_cast<const double*>(vals) : nullptr,
-        f64 ? nullptr : static_cast<const float*>(vals), keys_in, pairs_in, bad);
+        row_ptr, rows, row_at_d, colbase_d, count, keys_in, static_cast<const float*>(vals), keys_in, pairs_in, bad);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&b, bad, 8, cudaMemcpyDeviceToHost, s);

@@ -197,6 +197,10 @@ cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t
 // The same for `count` host arrays copied one after another into dst.
 cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t* bytes, size_t count,
                                cudaStream_t s);
+// The same for `count` arrays of doubles (counts[i] values each), narrowed to floats (round
+// to nearest, as a static_cast) while they are staged: half the bytes cross to the device.
+cudaError_t upload_staged_narrow(float* dst, const double* const* srcs, const size_t* counts, size_t count,
+                                 cudaStream_t s);
 // The rows of a device CSC's ratings (nnz entries) copied to host memory.
 cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s);
 // One rating set of one problem of a batch, row-major as for device_csc (row counts

@@ -103,7 +103,8 @@ typedef struct nomad_gpu_params {
                         * differ; batched form: the same for the CSCs and the large   *
                         * problems' visit bounds                                      */
   int32_t long_visit;  /* ASYNC: visits with at least this many ratings run the blocked
-                          (7-rating) path with TMA-staged rows; 0 = default 14        */
+                          (7-rating) path with TMA-staged rows; 0 = default 14 for
+                          FP32 rows, 17 for BF16_SR rows                             */
   int32_t priority_permille; /* ASYNC: columns with at least this many permille of the
                           largest column's ratings use the workers' priority queues;
                           0 = default 50, negative = no priority queue                */

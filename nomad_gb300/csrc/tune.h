@@ -8,6 +8,9 @@
 
 namespace nomad {
 
+// The ASYNC kernel's default long-visit length for the row type.
+inline int32_t default_long_visit(bool bf16) { return bf16 ? 17 : 14; }
+
 // Coordinate descent over the ASYNC kernel's runtime knobs: warps per block (the compiled
 // maximum -- what 0 asks for -- then two and four fewer), then the priority threshold
 // (25, 50, 100 permille, off), then the long-visit length (10, 14, 20), each stage
@@ -15,10 +18,11 @@ namespace nomad {
 // priority_permille, long_visit} and fills trial.status, trial.device_ms and
 // trial.warps_per_block (the count the kernel ran with).  A configuration is measured
 // once; failed trials (status != NOMAD_OK) never win.  Every trial is appended to `done`.
-// Returns false when no trial succeeded; else the winner in *wpb, *pri, *lv.
+// lv0 = 0 starts from lv_default (the context's default for the row type).  Returns false
+// when no trial succeeded; else the winner in *wpb, *pri, *lv.
 template <typename Measure>
 bool tune_descent(int32_t pri0, int32_t lv0, Measure&& measure, std::vector<nomad_gpu_tune_trial>& done,
-                  int32_t* wpb, int32_t* pri, int32_t* lv) {
+                  int32_t* wpb, int32_t* pri, int32_t* lv, int32_t lv_default = 14) {
   auto run = [&](int32_t w, int32_t p, int32_t l) -> double {
     for (const auto& t : done)
       if (t.warps_per_block == w && t.priority_permille == p && t.long_visit == l)
@@ -32,7 +36,7 @@ bool tune_descent(int32_t pri0, int32_t lv0, Measure&& measure, std::vector<noma
   };
   auto better = [](double a, double b) { return a >= 0 && (b < 0 || a < b); };
   *pri = pri0 == 0 ? 50 : pri0;  // the defaults, spelt out
-  *lv = lv0 > 0 ? lv0 : 14;
+  *lv = lv0 > 0 ? lv0 : lv_default;
   double best = run(0, *pri, *lv);
   const int32_t cap = done.back().status == NOMAD_OK ? done.back().warps_per_block : 0;
   *wpb = cap;

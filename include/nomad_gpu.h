@@ -112,7 +112,7 @@ typedef struct nomad_gpu_params {
   int32_t batch_share; /* batched form (exact = 0): a problem with at least this many
                           times one warp's fair share of the batch's ratings (and at
                           least 8,192) runs on a whole thread block of NOMAD workers;
-                          0 = default 4, negative = every problem on one warp        */
+                          0 = default 1, negative = every problem on one warp        */
   int32_t reserved[4];
 } nomad_gpu_params;
 

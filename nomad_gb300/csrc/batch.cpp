@@ -335,7 +335,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   std::vector<int32_t> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return nnz[x] > nnz[y]; });
-  // FMA form: problems with more than `batch_share` (default 4) warps' fair share of the
+  // FMA form: problems with more than `batch_share` (default 1) warps' fair share of the
   // ratings run on a whole block as NOMAD workers (rows split into kBatchWorkers blocks of
   // equal rating counts)
   int bps = 0;
@@ -347,7 +347,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   b->grid = bps * b->num_sms;
   const int64_t total = std::accumulate(nnz.begin(), nnz.end(), int64_t(0));
   const int64_t warps = static_cast<int64_t>(b->grid) * (p.exact ? nomad::kBatchThreads / 32 : nomad::kBatchWorkers);
-  const int64_t share = p.batch_share == 0 ? 4 : p.batch_share;
+  const int64_t share = p.batch_share == 0 ? 1 : p.batch_share;
   const int64_t big_min = share < 0 ? std::numeric_limits<int64_t>::max()
                                     : std::max<int64_t>(8192, share * total / std::max<int64_t>(warps, 1));
   int32_t n_big = 0;

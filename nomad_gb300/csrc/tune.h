@@ -66,16 +66,16 @@ bool tune_descent(int32_t pri0, int32_t lv0, Measure&& measure, std::vector<noma
 }
 
 // The batched form's large-problem threshold (params.batch_share): the starting share
-// (0 means the default 4) first, then every other share of {2, 4, 8, 16, never (-1)},
+// (0 means the default 1) first, then every other share of {1, 2, 4, 8, 16, never (-1)},
 // each measured once.  measure(trial) runs trial.batch_share and fills trial.status,
 // trial.device_ms and trial.large_problems; failed trials never win.  Every trial is
 // appended to `done`.  Returns false when no trial succeeded; else the winner in *share.
 template <typename Measure>
 bool batch_share_search(int32_t share0, Measure&& measure, std::vector<nomad_gpu_batch_tune_trial>& done,
                         int32_t* share) {
-  const int32_t first = share0 == 0 ? 4 : share0;
+  const int32_t first = share0 == 0 ? 1 : share0;
   std::vector<int32_t> order{first};
-  for (int32_t v : {2, 4, 8, 16, -1})
+  for (int32_t v : {1, 2, 4, 8, 16, -1})
     if (v != first) order.push_back(v);
   double best = -1.0;
   for (int32_t v : order) {

@@ -65,10 +65,11 @@ def test_search_on_synthetic_costs(tmp_path):
 def test_batch_autotune_picks_the_fastest_share(ng, gpu_ok):
     problems = [ng.synth_batch_problem(i, threads=1) for i in range(96)]
     best, trials = ng.batch_autotune(problems, epochs=2, lrate=0.002, drate=0.1, reg=0.05)
-    assert [t["batch_share"] for t in trials] == [4, 2, 8, 16, -1]
+    assert [t["batch_share"] for t in trials] == [1, 2, 4, 8, 16, -1]
     assert all(t["status"] == 0 and t["device_ms"] > 0 for t in trials)
     assert trials[-1]["large_problems"] == 0          # "never": every problem on one warp
-    assert trials[1]["large_problems"] >= trials[2]["large_problems"] >= trials[3]["large_problems"]
+    assert (trials[0]["large_problems"] >= trials[1]["large_problems"] >= trials[2]["large_problems"]
+            >= trials[3]["large_problems"])
     fastest = min(trials, key=lambda t: t["device_ms"])
     assert best["batch_share"] == fastest["batch_share"]
     nnz = sum(p[0].nnz for p in problems)

@@ -112,8 +112,8 @@ void case_batch_share() {
   int32_t share = 0;
   BatchModel m{8};
   CHECK(nomad::batch_share_search(0, m, done, &share));
-  CHECK(share == 8 && m.calls == 5 && done.size() == 5);
-  CHECK(done[0].batch_share == 4);  // the default first
+  CHECK(share == 8 && m.calls == 6 && done.size() == 6);
+  CHECK(done[0].batch_share == 1);  // the default first
   for (size_t i = 0; i < done.size(); ++i)
     for (size_t j = i + 1; j < done.size(); ++j) CHECK(done[i].batch_share != done[j].batch_share);
   done.clear();
@@ -123,12 +123,12 @@ void case_batch_share() {
   done.clear();
   BatchModel odd{3};  // a starting share outside the list is measured too
   CHECK(nomad::batch_share_search(3, odd, done, &share));
-  CHECK(share == 3 && done.size() == 6 && done[0].batch_share == 3);
+  CHECK(share == 3 && done.size() == 7 && done[0].batch_share == 3);
   done.clear();
   BatchModel failing{2};
   failing.fail_share = 2;  // the best share fails: the next best wins
   CHECK(nomad::batch_share_search(0, failing, done, &share));
-  CHECK(share == 4);
+  CHECK(share == 1);  // |1 - 2| = 1 beats |4 - 2| = 2
   struct Never {
     void operator()(nomad_gpu_batch_tune_trial& t) { t.status = NOMAD_ERR_TIMEOUT; }
   } never;

@@ -87,7 +87,9 @@ typedef struct nomad_gpu_params {
   int32_t device;      /* CUDA device ordinal                          default 0     */
   int32_t workers;     /* ASYNC: worker warps, 0 = every resident warp slot          */
   int32_t warps_per_block; /* 0 = auto                                               */
-  int32_t blocks_per_sm;   /* 0 = as many as fit                                     */
+  int32_t blocks_per_sm;   /* 0 = as many as fit; batched form: 1 or > 1 (four) blocks
+                              of its kernel per SM, 0 = four when no problem holds more
+                              than 2% of the batch's ratings, else one               */
   int32_t balance;     /* row blocks: 0 = equal rows (reference), 1 = equal ratings  */
   int32_t dsgd_inner_blocks; /* DSGD innerB (blocks per side), 0 = auto              */
   int32_t dsgd_strategy;     /* DSGD stratum strategy: 0 semi-WOR, 2 WOR             */

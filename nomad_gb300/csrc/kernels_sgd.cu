@@ -680,11 +680,11 @@ __device__ __forceinline__ void batch_large_problem(const nomad::BatchArgs& a, i
   __syncthreads();
 }
 
-// Four blocks per SM (64 warps, the SM's limit; 32 registers, a few spilled): a warp's
-// visit waits on its row loads, so residency sets the rate -- on the 4,096-problem batch
-// 1.20e9 / 2.02e9 / 2.59e9 / 2.80e9 fp32 updates/s at one to four blocks per SM.
-template <typename Store>
-__global__ void __launch_bounds__(nomad::kBatchWorkers * 32, 4) nomad_batch2_kernel(nomad::BatchArgs a) {
+// Built for one block per SM (74 / 86 registers) and for four (64 warps, the SM's limit;
+// 32 registers, a few spilled): a warp's visit waits on its row loads, so four blocks
+// carry more work at once, while one leaves the SM to a single large problem's workers.
+template <typename Store, int MB>
+__global__ void __launch_bounds__(nomad::kBatchWorkers * 32, MB) nomad_batch2_kernel(nomad::BatchArgs a) {
   constexpr int NV = 1;
   constexpr int E = Vec<Store>::E;
   __shared__ unsigned s_tail[nomad::kBatchWorkers];
@@ -835,7 +835,10 @@ cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s) {
 
 template <typename Store>
 static cudaError_t batch_epoch2_t(const BatchArgs& a, int grid, cudaStream_t s) {
-  nomad_batch2_kernel<Store><<<grid, kBatchWorkers * 32, 0, s>>>(a);
+  if (a.blocks_per_sm == 4)
+    nomad_batch2_kernel<Store, 4><<<grid, kBatchWorkers * 32, 0, s>>>(a);
+  else
+    nomad_batch2_kernel<Store, 1><<<grid, kBatchWorkers * 32, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   batch2_advance_kernel<<<1, 1, 0, s>>>(a.epoch, a.next, a.next_big, a.n_big);
@@ -846,9 +849,12 @@ cudaError_t launch_batch_epoch2(const BatchArgs& a, int grid, cudaStream_t s) {
   return a.bf16 ? batch_epoch2_t<__nv_bfloat16>(a, grid, s) : batch_epoch2_t<float>(a, grid, s);
 }
 
-cudaError_t batch2_occupancy(int bf16, int* bps) {
-  return bf16 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<__nv_bfloat16>,
-                                                              kBatchWorkers * 32, 0)
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<float>, kBatchWorkers * 32, 0);
+cudaError_t batch2_occupancy(int bf16, int blocks_per_sm, int* bps) {
+  constexpr int T = kBatchWorkers * 32;
+  if (blocks_per_sm == 4)
+    return bf16 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<__nv_bfloat16, 4>, T, 0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<float, 4>, T, 0);
+  return bf16 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<__nv_bfloat16, 1>, T, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, nomad_batch2_kernel<float, 1>, T, 0);
 }
 }  // namespace nomad

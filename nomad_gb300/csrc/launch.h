@@ -135,6 +135,7 @@ struct BatchArgs {
   unsigned* ring_ctr = nullptr;         // [grid x kBatchWorkers] ring counters (persist)
   int32_t* ctrl = nullptr;              // [2]: [1] device status (a large problem's wait ran out)
   int64_t budget_ns = 0;                // bound of a worker's idle wait inside a large problem
+  int32_t blocks_per_sm = 1;            // FMA form: the kernel's build, 1 or 4 blocks per SM
 };
 
 struct SseArgs {
@@ -241,7 +242,9 @@ cudaError_t batch_occupancy(int bf16, int exact, int* blocks_per_sm);
 // FMA form: blocks of kBatchWorkers warps; large problems first (a block each), then the
 // rest a warp each.
 cudaError_t launch_batch_epoch2(const BatchArgs& a, int grid, cudaStream_t s);
-cudaError_t batch2_occupancy(int bf16, int* blocks_per_sm);
+// blocks_per_sm selects the FMA kernel's build (1 or 4 resident blocks per SM); *bps is
+// how many of its blocks fit on an SM.
+cudaError_t batch2_occupancy(int bf16, int blocks_per_sm, int* bps);
 cudaError_t launch_batch_sse(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_dsgd_stratum(const DsgdArgs& a, int stratum, cudaStream_t s);
 cudaError_t launch_sse(const SseArgs& a, cudaStream_t s);

@@ -76,10 +76,11 @@ def test_batch_exact_equals_replay(ng, O, gpu_ok):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
-def test_batch_rmse_vs_fp64_oracle(ng, O, gpu_ok, precision):
+@pytest.mark.parametrize("blocks_per_sm", [1, 4])  # the FMA kernel's two builds
+def test_batch_rmse_vs_fp64_oracle(ng, O, gpu_ok, precision, blocks_per_sm):
     probs = small_batch(ng, count=12)
     epochs = 10
-    with ng.Batch(probs, lrate=LR, drate=DR, reg=REG, precision=precision) as b:
+    with ng.Batch(probs, lrate=LR, drate=DR, reg=REG, precision=precision, blocks_per_sm=blocks_per_sm) as b:
         b.epoch(epochs)
         _, te = b.rmse()
     for (train, test, dim, W0, H0), r in zip(probs, te):

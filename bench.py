@@ -418,7 +418,7 @@ def memory_workload_run(ng, device, epochs=2, need_gb=150.0, scale=1.0, forms=("
     return out
 
 
-def batched_run(ng, device, K, W, count=4096):
+def batched_run(ng, device, K, W, count=4096, blocks_per_sm=0):
     """The batched form: `count` independent problems of uneven shape and rank (m in
     [200, 20,000], n in [100, 5,000], density 0.5-5%, k in {16, 32, 64}), one CUDA-graph
     launch per epoch; compared with looping the single-problem path over a sample."""
@@ -427,7 +427,7 @@ def batched_run(ng, device, K, W, count=4096):
         probs = list(ex.map(lambda i: ng.synth_batch_problem(i, threads=1), range(count)))
     nnz = sum(p[0].nnz for p in probs)
     log(f"[bench] {count} problems ({nnz} train ratings) generated in {time.perf_counter() - t:.1f} s")
-    kw = dict(lrate=0.002, drate=0.1, reg=0.05, device=device)
+    kw = dict(lrate=0.002, drate=0.1, reg=0.05, device=device, blocks_per_sm=blocks_per_sm)
     res = {"workload": f"{count} problems, {nnz} train ratings: m logU[200, 20k], n logU[100, 5k], "
                        "density logU[0.5%, 5%], k in {16, 32, 64}, planted rank k/4",
            "lrate": 0.002, "drate": 0.1, "reg": 0.05, "steps": K, "warmup": W,
@@ -594,7 +594,7 @@ def main_batched(args, dist):
     launch per epoch; compared with looping the single-problem path over a sample."""
     import nomad_gb300 as ng
     K, W = args.steps, args.warmup
-    res = batched_run(ng, dist.local, K, W, args.count)
+    res = batched_run(ng, dist.local, K, W, args.count, args.bps)
     b = res["bf16"]
     print(json.dumps({
         "metric": "aggregate rating updates/s, batched independent problems", "value": b["updates_per_s"],

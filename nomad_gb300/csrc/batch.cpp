@@ -595,7 +595,7 @@ int init_impl(nomad_gpu_batch* b, const nomad_gpu_batch_problem* P, int32_t coun
   }
 
   trace.mark("factors");
-  b->sse_grid = std::max(1, std::min((b->a.n_parts + 3) / 4, 8 * b->num_sms));
+  b->sse_grid = std::max(1, std::min((b->a.n_parts + 3) / 4, 16 * b->num_sms));  // 4 warps a block
   RC(ensure_steps(b, 64));
   CK(cudaStreamSynchronize(b->stream));
   return NOMAD_OK;

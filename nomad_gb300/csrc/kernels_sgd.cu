@@ -545,18 +545,34 @@ __global__ void __launch_bounds__(nomad::kBatchThreads) batch_sse_kernel(nomad::
     float h[NV][E];
     load_col<Store, NV>(H, j, f, lane, h);
     double acc = 0.0;
-    for (int64_t o = pt.start; o < pt.end; ++o) {
-      if (cp[j + 1] <= o) {
-        do ++j;
-        while (cp[j + 1] <= o);
-        load_col<Store, NV>(H, j, f, lane, h);
+    // kU ratings at a time: their rows are loaded together, then the errors are summed in
+    // rating order (the same FP64 sum as one at a time)
+    constexpr int kU = 4;
+    for (int64_t o0 = pt.start; o0 < pt.end; o0 += kU) {
+      int2 r[kU];
+      typename Vec<Store>::Raw wr[kU][NV];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) r[u] = o0 + u < pt.end ? __ldg(&rt[o0 + u]) : make_int2(0, 0);
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+        if (o0 + u < pt.end) load_row_raw<Store, NV>(W, r[u].x, f.kpad, f.nvec, lane, wr[u]);
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int64_t o = o0 + u;
+        if (o < pt.end) {
+          if (cp[j + 1] <= o) {
+            do ++j;
+            while (cp[j + 1] <= o);
+            load_col<Store, NV>(H, j, f, lane, h);
+          }
+          float w[NV][E];
+#pragma unroll
+          for (int q = 0; q < NV; ++q) nd::unpack(wr[u][q], w[q]);
+          const float err = rating_error<Store, NV, false>(h, w, __int_as_float(r[u].y), f.nvec, f.red_width,
+                                                           f.dim, lane, nullptr);
+          acc += static_cast<double>(err) * err;
+        }
       }
-      const int2 r = __ldg(&rt[o]);
-      float w[NV][E];
-      load_row<Store, NV>(W, r.x, f.kpad, f.nvec, lane, w);
-      const float err = rating_error<Store, NV, false>(h, w, __int_as_float(r.y), f.nvec, f.red_width, f.dim,
-                                                       lane, nullptr);
-      acc += static_cast<double>(err) * err;
     }
     if (lane == 0) a.part_sse[part] = acc;
   }

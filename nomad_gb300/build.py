@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels_async.cu", "kernels_sgd.cu", "kernels_eval.cu", "csc_device.cu", "layout_device.cu"]
-CPP_SOURCES = ["ctx.cpp", "batch.cpp", "host_layout.cpp", "host_io.cpp", "host_synth.cpp"]
+CPP_SOURCES = ["ctx.cpp", "batch.cpp", "host_layout.cpp", "host_io.cpp", "host_synth.cpp", "host_stage.cpp"]
 CLI_SOURCES = ["nomad_main.cpp"]
 
 NVCC_FLAGS = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

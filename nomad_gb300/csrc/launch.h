@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "stage.h"
+
 namespace nomad {
 
 // Factor storage on the device: rows padded to `kpad` elements (a multiple of the
@@ -189,19 +191,6 @@ cudaError_t device_layout_fill(const int2* ratings, const int64_t* col_ptr, int6
                                int64_t* vl_ptr, int64_t* vl_ptr_host, int4* firsts_host, int32_t* max_seg,
                                cudaStream_t s);
 void device_layout_release(DeviceLayout* t, cudaStream_t s);
-// Host-to-device copy of pageable memory through two pinned staging buffers kept for the
-// life of the process (32 MB each, allocated on first use; uploads are serialised by a
-// lock): host threads fill one while the copy engine drains the other.  Returns when the
-// copies are done.  Copies straight from pageable memory ran ~30x slower when the host
-// had been under heavy allocation beforehand.
-cudaError_t upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s);
-// The same for `count` host arrays copied one after another into dst.
-cudaError_t upload_staged_many(void* dst, const void* const* srcs, const size_t* bytes, size_t count,
-                               cudaStream_t s);
-// The same for `count` arrays of doubles (counts[i] values each), narrowed to floats (round
-// to nearest, as a static_cast) while they are staged: half the bytes cross to the device.
-cudaError_t upload_staged_narrow(float* dst, const double* const* srcs, const size_t* counts, size_t count,
-                                 cudaStream_t s);
 // The rows of a device CSC's ratings (nnz entries) copied to host memory.
 cudaError_t device_csc_rows(const int2* ratings, int64_t nnz, int32_t* host_rows, cudaStream_t s);
 // One rating set of one problem of a batch, row-major as for device_csc (row counts

@@ -437,12 +437,14 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
       // visit lists on the device from the device CSC; the host keeps the row blocks and
       // builds the initial queues from each column's first visit
       RC(nomad::async_layout_rows(train, c->P, p.balance, L, threads));
+      trace.mark("  layout: row blocks (host)");
       nomad::DeviceLayout t;
       CK(nomad::device_layout_count(c->train, c->train_ptr, c->nnz_train, f.m, f.n, L.row_start.data(), c->P, group,
                                     pri_min, &t, c->stream));
       c->n_segments = t.nseg;
       RC(dalloc(c, &c->segs, static_cast<size_t>(t.nseg)));
       RC(dalloc(c, &c->vl_ptr, static_cast<size_t>(f.n) + 1));
+      trace.mark("  layout: visit allocations");
       L.vl_ptr.resize(static_cast<size_t>(f.n) + 1);
       std::vector<nomad::Segment> firsts(static_cast<size_t>(f.n));
       static_assert(sizeof(nomad::Segment) == sizeof(int4), "a visit is {start lo, start hi, len, owner}");
@@ -452,6 +454,7 @@ int init_impl(nomad_gpu_ctx* c, const nomad_gpu_problem* prob) {
                                    &max_seg, c->stream));
       L.max_segment = max_seg;
       nomad::async_layout_queues(train, pri_min, firsts.data(), L);
+      trace.mark("  layout: initial queues (host)");
       c->d2h_bytes += static_cast<int64_t>((static_cast<size_t>(f.n) + 1) * 8 + static_cast<size_t>(f.n) * 16);
       if (p.debug_flags & 4) RC(check_device_layout(c, train, p, pri_min, group, L, threads));
     } else {

@@ -12,6 +12,7 @@
 #include <climits>
 
 #include "launch.h"
+#include "trace.h"
 
 namespace {
 
@@ -173,6 +174,7 @@ cudaError_t device_layout_count(const int2* ratings, const int64_t* col_ptr, int
   *t = DeviceLayout{};
   if (nnz <= 0 || nnz > INT_MAX || m <= 0 || n <= 0 || P <= 0 || group <= 0 || group > kMaxGroup)
     return cudaErrorInvalidValue;
+  InitTrace trace;
   cudaError_t e = cudaSuccess;
   auto alloc = [&](void** p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMallocAsync(p, std::max<size_t>(bytes, 16), s);
@@ -187,6 +189,7 @@ cudaError_t device_layout_count(const int2* ratings, const int64_t* col_ptr, int
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(t->row_start, row_start, (static_cast<size_t>(P) + 1) * 4, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->flags + nnz, 0, 4, s);
+  if (trace.on && e == cudaSuccess) trace.mark("  layout: allocations", s);
   if (e == cudaSuccess) {
     row_worker_kernel<<<static_cast<unsigned>((m + 255) / 256), 256, 0, s>>>(t->row_start, P, m, t->row_worker);
     visit_flags_kernel<<<static_cast<unsigned>(n), 256, 0, s>>>(ratings, col_ptr, t->row_worker, group, priority_min,
@@ -197,6 +200,7 @@ cudaError_t device_layout_count(const int2* ratings, const int64_t* col_ptr, int
   int32_t total = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&total, t->seg_id + nnz, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (trace.on && e == cudaSuccess) trace.mark("  layout: visit flags and scan", s);
   t->nseg = total;
   if (e != cudaSuccess) device_layout_release(t, s);
   return e;
@@ -206,6 +210,7 @@ cudaError_t device_layout_fill(const int2* ratings, const int64_t* col_ptr, int6
                                bool group_routes, int64_t priority_min, uint64_t seed, DeviceLayout* t, int4* segs,
                                int64_t* vl_ptr, int64_t* vl_ptr_host, int4* firsts_host, int32_t* max_seg,
                                cudaStream_t s) {
+  InitTrace trace;
   cudaError_t e = cudaSuccess;
   int4 *in = nullptr, *firsts = nullptr;
   uint64_t* rkey = nullptr;
@@ -226,10 +231,12 @@ cudaError_t device_layout_fill(const int2* ratings, const int64_t* col_ptr, int6
                                                                 priority_min, in);
     visit_lens_kernel<<<static_cast<unsigned>((t->nseg + 255) / 256), 256, 0, s>>>(in, t->nseg, nnz, mx);
     vl_ptr_kernel<<<static_cast<unsigned>((n + 1 + 255) / 256), 256, 0, s>>>(col_ptr, t->seg_id, n, vl_ptr);
+    if (trace.on) trace.mark("  layout: allocations, visit starts and lengths", s);
     visit_routes_kernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(
         in, vl_ptr, col_ptr, n, group, group_routes, priority_min, seed, rkey, ridx, segs);
     e = cudaGetLastError();
   }
+  if (trace.on && e == cudaSuccess) trace.mark("  layout: routes", s);
   // the visit offsets and each column's first visit in route order, for the host's
   // initial queues
   if (e == cudaSuccess) {
@@ -241,11 +248,13 @@ cudaError_t device_layout_fill(const int2* ratings, const int64_t* col_ptr, int6
   int mxh = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&mxh, mx, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (trace.on && e == cudaSuccess) trace.mark("  layout: first visits, copies out", s);
   *max_seg = mxh;
   for (void* p : {static_cast<void*>(in), static_cast<void*>(rkey), static_cast<void*>(ridx), static_cast<void*>(mx),
                   static_cast<void*>(firsts)})
     if (p) cudaFreeAsync(p, s);
   device_layout_release(t, s);
+  if (trace.on && e == cudaSuccess) trace.mark("  layout: frees", s);
   return e;
 }
 

@@ -5,7 +5,7 @@
 //           of its column, or the first whose row leaves the previous owner's rows); the
 //           visit index of every rating by an exclusive scan of the flags;
 //   fill:   every visit {start, len, owner} in column order; each column's visit offset;
-//           then one thread per column puts its visits in route order.
+//           then one warp per column puts its visits in route order.
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -94,51 +94,155 @@ __global__ void vl_ptr_kernel(const int64_t* col_ptr, const int32_t* seg_id, int
   if (j <= n) vl_ptr[j] = seg_id[col_ptr[j]];
 }
 
-// One thread per column: its visits (in column order in `in`) into route order in `out`,
-// as the host build orders them.  Hierarchical routes: runs of one group's visits ordered
-// by the group key, inside a run by the worker key, both as (key, index) pairs; runs are
-// sorted in `rkey`/`ridx` (scratch at the column's visit offset), a run's visits in
-// registers (at most kMaxGroup).  Otherwise a Fisher-Yates shuffle by the column's stream.
+// A column's visits (in column order in `s`) into route order in `d`, as the host build
+// orders them.  Hierarchical routes: runs of one group's visits ordered by the group key,
+// inside a run by the worker key, both as (key, index) pairs.  Otherwise a Fisher-Yates
+// shuffle by the column's stream.
 constexpr int kMaxGroup = 32;
-__global__ void visit_routes_kernel(const int4* in, const int64_t* vl_ptr, const int64_t* col_ptr, int32_t n,
-                                    int32_t group, bool group_routes, int64_t priority_min, uint64_t seed,
-                                    uint64_t* rkey, int32_t* ridx, int4* out) {
-  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+
+// The runs sorted by insertion in `key`/`idx` (scratch at the column's visit offset), a
+// run's visits in registers (at most kMaxGroup): one thread.
+__device__ void group_route_serial(const int4* s, int4* d, int64_t k, int32_t group, uint64_t kb, uint64_t kw,
+                                   uint64_t* key, int32_t* idx) {
+  int64_t nr = 0;
+  for (int64_t i = 0; i < k; ++i)
+    if (i == 0 || s[i].w / group != s[i - 1].w / group) {
+      // insertion into the sorted runs
+      const uint64_t kk = mix64(kb ^ static_cast<uint64_t>(s[i].w / group));
+      int64_t p = nr++;
+      while (p > 0 && (key[p - 1] > kk || (key[p - 1] == kk && idx[p - 1] > i))) {
+        key[p] = key[p - 1];
+        idx[p] = idx[p - 1];
+        --p;
+      }
+      key[p] = kk;
+      idx[p] = static_cast<int32_t>(i);
+    }
+  int64_t o = 0;
+  for (int64_t r = 0; r < nr; ++r) {
+    const int64_t b = idx[r];
+    int64_t e = b + 1;
+    while (e < k && s[e].w / group == s[b].w / group) ++e;
+    uint64_t ik[kMaxGroup];
+    int32_t ii[kMaxGroup];
+    int c = 0;
+    for (int64_t i = b; i < e; ++i) {
+      const uint64_t kk = mix64(kw ^ static_cast<uint64_t>(s[i].w));
+      int p = c++;
+      while (p > 0 && (ik[p - 1] > kk || (ik[p - 1] == kk && ii[p - 1] > i))) {
+        ik[p] = ik[p - 1];
+        ii[p] = ii[p - 1];
+        --p;
+      }
+      ik[p] = kk;
+      ii[p] = static_cast<int32_t>(i);
+    }
+    for (int x = 0; x < c; ++x) d[o++] = s[ii[x]];
+  }
+}
+
+// One warp per column.  Hierarchical routes with at most kRunCap runs are ordered by the
+// whole warp: run starts found by ballot; each run's rank by (group key, start) counted
+// against every other run; the runs' output offsets by an exclusive sum of their lengths
+// in rank order; each run's visits sorted by (worker key, index) on one lane.  The same
+// order as group_route_serial, which lane 0 runs for columns with more runs, as it runs
+// the Fisher-Yates shuffle.
+constexpr int kRouteWarps = 4;
+constexpr int kRunCap = 256;
+
+__global__ void __launch_bounds__(kRouteWarps * 32)
+    visit_routes_kernel(const int4* in, const int64_t* vl_ptr, const int64_t* col_ptr, int32_t n, int32_t group,
+                        bool group_routes, int64_t priority_min, uint64_t seed, uint64_t* rkey, int32_t* ridx,
+                        int4* out) {
+  __shared__ uint64_t s_key[kRouteWarps][kRunCap];
+  __shared__ int32_t s_start[kRouteWarps][kRunCap];
+  __shared__ int32_t s_off[kRouteWarps][kRunCap + 1];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * kRouteWarps + wib;
+  if (j >= n) return;  // the whole warp
   const int64_t v0 = vl_ptr[j];
   const int64_t k = vl_ptr[j + 1] - v0;
   if (k == 0) return;
   const int4* s = in + v0;
   int4* d = out + v0;
   const bool pri = is_priority(col_ptr, j, priority_min);
-  if (group_routes && !pri && group > 1 && k > 1) {
-    const uint64_t kb = stream_key64(seed, 149, static_cast<uint64_t>(j));
-    const uint64_t kw = stream_key64(seed, 151, static_cast<uint64_t>(j));
-    uint64_t* key = rkey + v0;
-    int32_t* idx = ridx + v0;
-    int64_t nr = 0;
-    for (int64_t i = 0; i < k; ++i)
-      if (i == 0 || s[i].w / group != s[i - 1].w / group) {
-        // insertion into the sorted runs
-        const uint64_t kk = mix64(kb ^ static_cast<uint64_t>(s[i].w / group));
-        int64_t p = nr++;
-        while (p > 0 && (key[p - 1] > kk || (key[p - 1] == kk && idx[p - 1] > i))) {
-          key[p] = key[p - 1];
-          idx[p] = idx[p - 1];
-          --p;
-        }
-        key[p] = kk;
-        idx[p] = static_cast<int32_t>(i);
+  if (!(group_routes && !pri && group > 1 && k > 1)) {
+    if (lane == 0) {
+      for (int64_t i = 0; i < k; ++i) d[i] = s[i];
+      uint64_t st = stream_key64(seed, 137, static_cast<uint64_t>(j));
+      for (int64_t i = k - 1; i > 0; --i) {
+        st += 0x9E3779B97F4A7C15ULL;
+        const uint64_t t = __umul64hi(mix64(st), static_cast<uint64_t>(i + 1));
+        const int4 a = d[i];
+        d[i] = d[t];
+        d[t] = a;
       }
-    int64_t o = 0;
-    for (int64_t r = 0; r < nr; ++r) {
-      const int64_t b = idx[r];
-      int64_t e = b + 1;
-      while (e < k && s[e].w / group == s[b].w / group) ++e;
+    }
+    return;
+  }
+  const uint64_t kb = stream_key64(seed, 149, static_cast<uint64_t>(j));
+  const uint64_t kw = stream_key64(seed, 151, static_cast<uint64_t>(j));
+  uint64_t* skey = s_key[wib];
+  int32_t* sstart = s_start[wib];
+  int32_t* soff = s_off[wib];
+  // run starts, in index order
+  int nr = 0;
+  for (int64_t i0 = 0; i0 < k; i0 += 32) {
+    const int64_t i = i0 + lane;
+    bool st = false;
+    int32_t g = 0;
+    if (i < k) {
+      g = s[i].w / group;
+      st = i == 0 || s[i - 1].w / group != g;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, st);
+    const int pos = nr + __popc(bal & ((1u << lane) - 1u));
+    if (st && pos < kRunCap) {
+      skey[pos] = mix64(kb ^ static_cast<uint64_t>(g));
+      sstart[pos] = static_cast<int32_t>(i);
+    }
+    nr += __popc(bal);
+  }
+  __syncwarp();
+  if (nr > kRunCap) {
+    if (lane == 0) group_route_serial(s, d, k, group, kb, kw, rkey + v0, ridx + v0);
+    return;
+  }
+  constexpr int kPer = kRunCap / 32;
+  int rk[kPer];
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    const int r = lane + 32 * t;
+    rk[t] = 0;
+    if (r < nr) {
+      const uint64_t kr = skey[r];
+      const int32_t br = sstart[r];
+      int rank = 0;
+      for (int q = 0; q < nr; ++q) {
+        const uint64_t kq = skey[q];
+        rank += (kq < kr || (kq == kr && sstart[q] < br)) ? 1 : 0;
+      }
+      rk[t] = rank;
+      soff[rank + 1] = (r + 1 < nr ? sstart[r + 1] : static_cast<int32_t>(k)) - br;  // the run's length
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {  // offsets in rank order: exclusive sum of the lengths
+    soff[0] = 0;
+    for (int q = 1; q <= nr; ++q) soff[q] += soff[q - 1];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    const int r = lane + 32 * t;
+    if (r < nr) {
+      const int64_t b = sstart[r];
+      const int64_t e = r + 1 < nr ? sstart[r + 1] : k;
       uint64_t ik[kMaxGroup];
       int32_t ii[kMaxGroup];
       int c = 0;
-      for (int64_t i = b; i < e; ++i) {
+      for (int64_t i = b; i < e && c < kMaxGroup; ++i) {
         const uint64_t kk = mix64(kw ^ static_cast<uint64_t>(s[i].w));
         int p = c++;
         while (p > 0 && (ik[p - 1] > kk || (ik[p - 1] == kk && ii[p - 1] > i))) {
@@ -149,17 +253,8 @@ __global__ void visit_routes_kernel(const int4* in, const int64_t* vl_ptr, const
         ik[p] = kk;
         ii[p] = static_cast<int32_t>(i);
       }
-      for (int x = 0; x < c; ++x) d[o++] = s[ii[x]];
-    }
-  } else {
-    for (int64_t i = 0; i < k; ++i) d[i] = s[i];
-    uint64_t st = stream_key64(seed, 137, static_cast<uint64_t>(j));
-    for (int64_t i = k - 1; i > 0; --i) {
-      st += 0x9E3779B97F4A7C15ULL;
-      const uint64_t t = __umul64hi(mix64(st), static_cast<uint64_t>(i + 1));
-      const int4 a = d[i];
-      d[i] = d[t];
-      d[t] = a;
+      int4* o = d + soff[rk[t]];
+      for (int x = 0; x < c; ++x) o[x] = s[ii[x]];
     }
   }
 }
@@ -232,7 +327,7 @@ cudaError_t device_layout_fill(const int2* ratings, const int64_t* col_ptr, int6
     visit_lens_kernel<<<static_cast<unsigned>((t->nseg + 255) / 256), 256, 0, s>>>(in, t->nseg, nnz, mx);
     vl_ptr_kernel<<<static_cast<unsigned>((n + 1 + 255) / 256), 256, 0, s>>>(col_ptr, t->seg_id, n, vl_ptr);
     if (trace.on) trace.mark("  layout: allocations, visit starts and lengths", s);
-    visit_routes_kernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(
+    visit_routes_kernel<<<static_cast<unsigned>((n + kRouteWarps - 1) / kRouteWarps), kRouteWarps * 32, 0, s>>>(
         in, vl_ptr, col_ptr, n, group, group_routes, priority_min, seed, rkey, ridx, segs);
     e = cudaGetLastError();
   }
